@@ -1,0 +1,396 @@
+"""Benchmark of the SpMM hot path on GB300.
+
+Workload (one "step"): C = A @ B with the merge-path CSR SpMM, A the
+reddit-shaped power-law graph (232,965 nodes, ~114.6M directed edges,
+Chung-Lu, exponent 1.8, degrees capped at 20,000, values D^-1/2 A D^-1/2 in
+FP32), B 232,965 x 256 FP32 N(0,1).  Inputs are synthetic and seeded (the
+reference's reddit.mtx is not distributed).
+
+metric: SpMM achieved GB/s by the gather model -- every nonzero reads one
+whole feature row: bytes = 4(n+1) + 8 nnz + nnz*F*sizeof(B) + n*F*4 -- per
+launch, divided by the launch's CUDA-event time.  L2 is flushed (a 512 MiB
+write) before every timed step.  Extra keys: BF16-feature time, errors vs
+FP64 on sampled rows, the end-to-end number through the public API with host
+buffers, the CPU baseline, clocks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SpMM achieved HBM GB/s (% of peak), fwd+bwd time BF16 vs FP32 at stated error"
+WORKLOAD = "reddit_like_csr_spmm_f256"
+
+
+def gather_bytes(n, nnz, F, bsz):
+    return 4 * (n + 1) + 8 * nnz + nnz * F * bsz + n * F * 4
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the SpMM kernel from the committed ncu
+    summary (None until one exists)."""
+    p = ROOT / "profiles" / "csr_spmm_reddit_f256.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_inputs(device):
+    import torch
+    from spmm_eval_gb300 import graphs as G
+    g = G.gcn_normalize(G.reddit_like(device=device))
+    B = G.normal(0x5EED + 4, 9, (g.ncols, 256), device=device)
+    return g, B
+
+
+def sample_rows_for_error(g, k=192):
+    import torch
+    deg = (g.rowptr[1:] - g.rowptr[:-1]).to("cpu")
+    top = torch.topk(deg, 32).indices
+    spread = torch.linspace(0, g.nrows - 1, k - 32).long()
+    return torch.unique(torch.cat([top, spread]))
+
+
+def fp64_rows(g_cpu, B_cpu, rows):
+    """FP64 products and |A||B| magnitudes of the sampled rows (torch CPU)."""
+    import torch
+    out, mag = [], []
+    Bd = B_cpu.double()
+    for r in rows.tolist():
+        s, e = int(g_cpu.rowptr[r]), int(g_cpu.rowptr[r + 1])
+        cols = g_cpu.colind[s:e].long()
+        v = g_cpu.vals[s:e].double()
+        out.append(v @ Bd[cols])
+        mag.append(v.abs() @ Bd[cols].abs())
+    return torch.stack(out), torch.stack(mag)
+
+
+def rel_err(got, ref, mag):
+    d = (got.double() - ref).abs()
+    r = d / mag.clamp_min(1e-300)
+    return float(r.max()), float(r.mean())
+
+
+def cpu_baseline(g_cpu, B_cpu, budget_s=10.0):
+    """OpenMP FP32 CSR SpMM of the oracle on a bounded row sample."""
+    import numpy as np
+    import oracle
+    rp = g_cpu.rowptr.numpy()
+    target = 4_000_000
+    r1 = int(np.searchsorted(rp, target))
+    r1 = max(1, min(r1, g_cpu.nrows))
+    nnz = int(rp[r1])
+    ci, va, Bn = g_cpu.colind.numpy(), g_cpu.vals.numpy(), B_cpu.numpy()
+    threads = oracle.max_threads()
+    oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)  # warm-up
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while True:
+        t0 = time.perf_counter()
+        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() > t_end or len(times) >= 50:
+            break
+    t = statistics.median(times)
+    gb = gather_bytes(r1, nnz, B_cpu.shape[1], 4) / 1e9
+    return {"value": round(gb / t, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"rows [0,{r1}) = {nnz} nonzeros of the same graph, F=256 FP32, "
+                      f"median of {len(times)} passes ({t*1e3:.1f} ms/pass)"}, t
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    """The reference has no CPU path of its own; its semantics are timed as
+    the oracle's OpenMP FP32 CSR SpMM on the host cores (rank 0 only)."""
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    import torch
+    import oracle
+    oracle.build()
+    dev = torch.device(f"cuda:{local}") if torch.cuda.is_available() else torch.device("cpu")
+    g, B = make_inputs(dev)
+    g_cpu, B_cpu = g.to("cpu"), B.to("cpu")
+    del g, B
+    import numpy as np
+    rp = g_cpu.rowptr.numpy()
+    r1 = int(np.searchsorted(rp, 4_000_000))
+    nnz = int(rp[r1])
+    ci, va, Bn = g_cpu.colind.numpy(), g_cpu.vals.numpy(), B_cpu.numpy()
+    for _ in range(args.warmup):
+        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+        times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    gb = gather_bytes(r1, nnz, 256, 4) / 1e9
+    value = gb / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nodes": g_cpu.nrows, "nnz": g_cpu.nnz, "F": 256,
+                   "sample_rows": r1, "sample_nnz": nnz},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": oracle.max_threads(),
+                         "kind": "port",
+                         "sample": f"rows [0,{r1}) = {nnz} nonzeros per step, F=256 FP32"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from spmm_eval_gb300 import ops
+    world, rank, local = dist_setup(args)
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    g, B = make_inputs(dev)
+    n, nnz, F = g.nrows, g.nnz, 256
+    A = ops.CSR(g.rowptr, g.colind, g.vals, n, n)
+    Bh = B.to(torch.bfloat16)
+    C = torch.empty((n, F), dtype=torch.float32, device=dev)
+    Ch = torch.empty_like(C)
+    ws = ops.SpmmWorkspace()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def step_f32():
+        ops.csr_spmm(A, B, out=C, workspace=ws)
+
+    def step_bf16():
+        ops.csr_spmm(A, Bh, out=Ch, workspace=ws)
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for s, e in evs:
+            flush.zero_()
+            s.record(stream)
+            fn()
+            e.record(stream)
+        torch.cuda.synchronize(dev)
+        return [s.elapsed_time(e) for s, e in evs]
+
+    for _ in range(max(3, args.warmup)):
+        step_f32()
+        step_bf16()
+    torch.cuda.synchronize(dev)
+
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev.index if dev.index is not None else 0) as clk:
+        t0 = time.perf_counter()
+        ms = timed(step_f32, args.steps)
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    ms_f32 = sum(ms) / len(ms)
+    ms_f32 = max_over_ranks(ms_f32, world, dev)
+    ms_bf16 = sum(timed(step_bf16, args.steps)) / args.steps
+
+    bytes_f32 = gather_bytes(n, nnz, F, 4)
+    bytes_bf16 = gather_bytes(n, nnz, F, 2)
+    value = world * bytes_f32 / (ms_f32 * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profile_traffic()
+
+    # errors vs FP64 on sampled rows (incl. the 32 largest hubs)
+    rows = sample_rows_for_error(g)
+    g_cpu = g.to("cpu")
+    B_cpu = B.to("cpu")
+    ref, mag = fp64_rows(g_cpu, B_cpu, rows)
+    e32 = rel_err(C[rows.to(dev)].cpu(), ref, mag)
+    e16 = rel_err(Ch[rows.to(dev)].cpu(), ref, mag)
+
+    # end to end through the public API from pinned host buffers
+    h_rowptr = g_cpu.rowptr.pin_memory()
+    h_colind = g_cpu.colind.pin_memory()
+    h_vals = g_cpu.vals.pin_memory()
+    h_B = B_cpu.pin_memory()
+    h_C = torch.empty((n, F), dtype=torch.float32).pin_memory()
+    d_rowptr, d_colind, d_vals = torch.empty_like(g.rowptr), torch.empty_like(g.colind), torch.empty_like(g.vals)
+    d_B = torch.empty_like(B)
+
+    def e2e_step():
+        d_rowptr.copy_(h_rowptr, non_blocking=True)
+        d_colind.copy_(h_colind, non_blocking=True)
+        d_vals.copy_(h_vals, non_blocking=True)
+        d_B.copy_(h_B, non_blocking=True)
+        ops.csr_spmm(ops.CSR(d_rowptr, d_colind, d_vals, n, n), d_B, out=C, workspace=ws)
+        h_C.copy_(C, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    e2e_steps = max(3, min(args.steps, 10))
+    ms_e2e = sum(timed(e2e_step, e2e_steps)) / e2e_steps
+    ms_e2e = max_over_ranks(ms_e2e, world, dev)
+    h2d = (h_rowptr.numel() * 4 + h_colind.numel() * 4 + h_vals.numel() * 4 + h_B.numel() * 4)
+    d2h = h_C.numel() * 4
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, _ = cpu_baseline(g_cpu, B_cpu)
+
+    if rank != 0:
+        return
+    achieved = bytes_f32 / (ms_f32 * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_f32, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nodes": n, "nnz": nnz, "F": F,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed before every timed step (512 MiB write)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per launch",
+                     "bytes_per_launch": bytes_f32},
+        "bf16": {"ms_per_step": round(ms_bf16, 4),
+                 "gbs_gather_model": round(bytes_bf16 / (ms_bf16 * 1e-3) / 1e9, 1),
+                 "speedup_vs_f32": round(ms_f32 / ms_bf16, 3)},
+        "error_vs_fp64": {"rows_sampled": int(rows.numel()),
+                          "scale": "|C-C64| / (|A| |B|) elementwise",
+                          "f32": {"max": e32[0], "mean": e32[1]},
+                          "bf16_features": {"max": e16[0], "mean": e16[1]}},
+        "e2e": {"value": round(world * bytes_f32 / (ms_e2e * 1e-3) / 1e9, 2), "unit": "GB/s",
+                "ms_per_step": round(ms_e2e, 3), "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "timed_region_wall_s": round(wall, 3),
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,100 @@
+/*
+ * gbspmm.h -- C ABI of the GB300 (sm_103a) SpMM library.
+ *
+ * Drop-in boundary for the SpMM evaluation path of spmm_eval.  Every entry
+ * point takes plain device pointers, sizes and a CUDA stream, returns a
+ * gbs_status, never traps on the device and never synchronises the device
+ * unless its comment says so (a size that must reach the host).
+ *
+ * Conventions
+ *   - CSR matrices use int32 row pointers / column indices, zero based, with
+ *     the column indices of a row ascending (what coo2csr in the reference's
+ *     backend/readMtx.hpp:246-304 produces).
+ *   - Dense feature matrices (B, C, dC, X) are row-major, leading dimension F.
+ *   - The caller owns every input, output and workspace buffer.  Opaque
+ *     objects (gbs_csr_transpose) are created and destroyed explicitly.
+ *   - gbs_stream_t is a cudaStream_t; NULL is the legacy default stream.
+ *   - Errors: a non-zero gbs_status; gbs_last_error() gives a message for the
+ *     calling thread.
+ */
+#ifndef GBSPMM_H_
+#define GBSPMM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBS_API __attribute__((visibility("default")))
+#else
+#define GBS_API
+#endif
+
+typedef struct CUstream_st *gbs_stream_t;
+
+typedef enum gbs_status {
+  GBS_OK = 0,
+  GBS_ERR_INVALID_ARG = 1, /* bad size, null pointer, malformed CSR      */
+  GBS_ERR_UNSUPPORTED = 2, /* valid request this build does not support  */
+  GBS_ERR_CUDA = 3,        /* a CUDA runtime call failed                 */
+  GBS_ERR_OOM = 4,         /* device allocation failed                   */
+  GBS_ERR_INTERNAL = 5
+} gbs_status;
+
+/* Element type of a dense feature / gradient matrix.  Accumulation is
+ * always FP32 and outputs are FP32. */
+typedef enum gbs_dtype { GBS_F32 = 0, GBS_BF16 = 1, GBS_F16 = 2 } gbs_dtype;
+
+/* Message describing the last failure on the calling thread ("" if none). */
+GBS_API const char *gbs_last_error(void);
+/* ABI version of this header (bumped on incompatible change). */
+GBS_API int gbs_abi_version(void);
+
+/* ------------------------------------------------------------------------
+ * CSR SpMM  C = A * B   (A: nrows x ncols CSR, B: ncols x F, C: nrows x F)
+ *
+ * Replaces the cuSPARSE call of evalCSRSpmmFloatCuSPARSE
+ * (test_spmm_full.cu:212-342: cusparseSpMM, CSR, alpha = 1, beta = 0) with
+ * row-major B and C instead of the column-major copies made at :215-223 and
+ * :321-329.  C is overwritten (every row, including empty ones).
+ *
+ * Schedule: merge-path over (rows + nonzeros); each warp owns an equal share
+ * and a row cut by a share boundary is finished by whichever warp arrives
+ * last at it (no spin-waits), summing the pieces in a fixed order, so the
+ * result is deterministic for a given device and F.
+ *
+ * vals may be NULL: every stored entry then counts as 1.0 (binary A).
+ * B may be FP32, BF16 or FP16 (btype); accumulation and C are FP32.
+ * ------------------------------------------------------------------------ */
+
+/* Bytes of workspace gbs_csr_spmm needs for this shape on the current
+ * device.  The workspace must be zero-filled before its first use
+ * (gbs_csr_spmm_workspace_init); every call leaves it zero-filled again.
+ * A workspace must not be used by two calls that can overlap on the GPU. */
+GBS_API gbs_status gbs_csr_spmm_workspace_size(int nrows, int nnz, int F,
+                                       gbs_dtype btype, size_t *bytes);
+GBS_API gbs_status gbs_csr_spmm_workspace_init(void *d_workspace, size_t bytes,
+                                       gbs_stream_t stream);
+
+GBS_API gbs_status gbs_csr_spmm(int nrows, int ncols, int nnz, const int *d_rowptr,
+                        const int *d_colind, const float *d_vals,
+                        const void *d_B, gbs_dtype btype, int F, float *d_C,
+                        void *d_workspace, size_t workspace_bytes,
+                        gbs_stream_t stream);
+
+/* One-call FP32 form with the argument meaning of the cuSPARSE generic
+ * SpMM used by the reference (alpha = 1, beta = 0, FP32 everywhere).
+ * Allocates and frees its workspace with stream-ordered allocation. */
+GBS_API gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz,
+                            const int *d_rowptr, const int *d_colind,
+                            const float *d_vals, const float *d_B, int F,
+                            float *d_C, gbs_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSPMM_H_ */

@@ -1,0 +1,81 @@
+"""ctypes binding of ``lib/libgbspmm.so`` (the C ABI in ``include/gbspmm.h``).
+
+The shared library is the only compute path: if it is missing this module
+raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgbspmm.so"
+
+GBS_OK, GBS_ERR_INVALID_ARG, GBS_ERR_UNSUPPORTED, GBS_ERR_CUDA, GBS_ERR_OOM, GBS_ERR_INTERNAL = range(6)
+GBS_F32, GBS_BF16, GBS_F16 = 0, 1, 2
+
+_STATUS_NAMES = {
+    GBS_OK: "GBS_OK",
+    GBS_ERR_INVALID_ARG: "GBS_ERR_INVALID_ARG",
+    GBS_ERR_UNSUPPORTED: "GBS_ERR_UNSUPPORTED",
+    GBS_ERR_CUDA: "GBS_ERR_CUDA",
+    GBS_ERR_OOM: "GBS_ERR_OOM",
+    GBS_ERR_INTERNAL: "GBS_ERR_INTERNAL",
+}
+
+p = C.c_void_p
+i32 = C.c_int
+i64 = C.c_int64
+sz = C.c_size_t
+st = C.c_int  # gbs_status
+pi32 = C.POINTER(C.c_int)
+psz = C.POINTER(C.c_size_t)
+
+# name -> (restype, argtypes); every entry point declared in include/gbspmm.h
+SIGNATURES: dict[str, tuple] = {
+    "gbs_last_error": (C.c_char_p, []),
+    "gbs_abi_version": (C.c_int, []),
+    "gbs_csr_spmm_workspace_size": (st, [i32, i32, i32, i32, psz]),
+    "gbs_csr_spmm_workspace_init": (st, [p, sz, p]),
+    "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),
+    "gbs_csr_spmm_f32": (st, [i32, i32, i32, p, p, p, p, i32, p, p]),
+}
+
+
+class GbsError(RuntimeError):
+    """A non-zero gbs_status returned by the library."""
+
+    def __init__(self, status: int, where: str, message: str):
+        self.status = status
+        super().__init__(f"{where}: {_STATUS_NAMES.get(status, status)}: {message}")
+
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+
+def load() -> C.CDLL:
+    """Load libgbspmm.so once and attach the argument types."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{LIB_PATH} is not built; run spmm_eval_gb300.build.build() "
+                    "(there is no CPU fallback for any operation)")
+            lib = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def call(name: str, *args) -> None:
+    """Call an entry point and raise GbsError on a non-zero status."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != GBS_OK:
+        msg = lib.gbs_last_error().decode(errors="replace")
+        raise GbsError(rc, name, msg)

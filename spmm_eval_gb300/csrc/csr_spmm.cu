@@ -1,0 +1,425 @@
+// CSR SpMM C = A * B on sm_103a: merge-path schedule over rows + nonzeros,
+// warp-wide 16-byte gathers of feature rows, FP32 accumulation.
+//
+// Replaces cusparseSpMM in evalCSRSpmmFloatCuSPARSE (test_spmm_full.cu:279-307:
+// CSR A, alpha = 1, beta = 0, FP32) for row-major B and C.
+//
+// Schedule.  The merge of the row-end list rowptr[1..n] with the nonzero
+// indices 0..nnz-1 has n + nnz events; warp w owns events [w*D, (w+1)*D).
+// A row whose events all fall in one warp is summed by that warp in CSR
+// order and written to C directly.  A row cut by a share boundary is summed
+// piecewise: every warp holding a piece writes it to a workspace slot, bumps
+// a per-row arrival counter, and the warp that arrives last adds the pieces
+// in warp order and writes C (then resets the counter).  Nothing waits on
+// another warp, and the addition order depends only on (n, nnz, P), so the
+// result is bitwise reproducible for a given device and F.
+//
+// Lane mapping.  A feature row of F elements is nvec = F / VEC 16-byte
+// chunks.  LPR = min(32, pow2 >= nvec) lanes cover one row (CH chunks each);
+// the NSUB = 32 / LPR sub-groups of a warp take interleaved nonzeros of the
+// same row and are folded together with xor-shuffles at the row end.
+#include <mutex>
+
+#include "common.cuh"
+#include "csr_spmm.cuh"
+#include "feat.cuh"
+
+namespace gbs {
+
+struct MergeArgs {
+  int nrows, nnz, F, nvec;
+  const int *rowptr;
+  const int *colind;
+  const float *vals;  // may be null: binary A
+  const void *B;
+  float *C;
+  float *partials;  // [2P][ldp]
+  int *counters;    // [P]
+  int ldp;
+  int P;
+  long long D;
+};
+
+// Largest i in [0, n] with rowptr[i] + i <= d (rows finished at merge
+// diagonal d).
+__device__ __forceinline__ int merge_search(const int *__restrict__ rowptr, int n, int nnz,
+                                            long long d) {
+  long long lo = d - nnz;
+  if (lo < 0) lo = 0;
+  long long hi = d < n ? d : n;
+  while (lo < hi) {
+    long long mid = (lo + hi + 1) >> 1;
+    if ((long long)__ldg(rowptr + mid) + mid <= d) lo = mid;
+    else hi = mid - 1;
+  }
+  return (int)lo;
+}
+
+template <int DT, int VEC, int LPR, int CH, int U>
+struct MergeKernel {
+  static constexpr int NSUB = 32 / LPR;
+  static constexpr int KPS = LPR;  // nonzeros per sub-group in a batch of 32
+  using F_ = Feat<DT, VEC>;
+  using raw = typename F_::raw;
+
+  // Sum nonzeros [jb, je) of one row into acc (this lane's columns, this
+  // lane's sub-group share).
+  static __device__ __forceinline__ void accumulate(const MergeArgs &a, int jb, int je,
+                                                    int lane, float (&acc)[CH][VEC]) {
+    const int sub = lane / LPR;
+    const int sl = lane % LPR;
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
+
+    for (int base = jb; base < je; base += 32) {
+      const int n_valid = min(32, je - base);
+      int my_col = 0;
+      float my_val = 0.f;
+      if (lane < n_valid) {
+        my_col = ld_stream_i32(a.colind + base + lane);
+        my_val = a.vals ? ld_stream_f32(a.vals + base + lane) : 1.f;
+      }
+      // blocked summation: each batch of 32 nonzeros is summed into a fresh
+      // partial that is then added to the row total (error ~ sqrt(32) +
+      // sqrt(deg/32) roundings instead of sqrt(deg))
+      float bs[CH][VEC];
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) bs[c][q] = 0.f;
+      for (int u0 = 0; u0 < KPS; u0 += U) {
+        if (u0 * NSUB >= n_valid) break;
+        raw bv[U][CH];
+        float vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int k = (u0 + u) * NSUB + sub;
+          const int col = __shfl_sync(0xffffffffu, my_col, k);
+          const float v = __shfl_sync(0xffffffffu, my_val, k);
+          const bool ok = k < n_valid;
+          vv[u] = ok ? v : 0.f;
+          const size_t rowbase = (size_t)col * (size_t)a.F;
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            const int chunk = c * LPR + sl;
+            if (ok && chunk < a.nvec) bv[u][c] = F_::load(a.B, rowbase + (size_t)chunk * VEC);
+            else bv[u][c] = F_::zero();
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) acc[c][q] += bs[c][q];
+    }
+    // fold the sub-groups (fixed tree order)
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1)
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) acc[c][q] += __shfl_xor_sync(0xffffffffu, acc[c][q], off);
+  }
+
+  template <bool STREAM>
+  static __device__ __forceinline__ void write_row(const MergeArgs &a, float *dst, int lane,
+                                                   const float (&acc)[CH][VEC]) {
+    if (lane >= LPR) return;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + lane;
+      if (chunk < a.nvec) store_vec<VEC, STREAM>(dst + (size_t)chunk * VEC, acc[c]);
+    }
+  }
+
+  // Called by every warp holding a piece of a split row r after it has
+  // written that piece to its head or tail slot.  The last of the (w2 - w1 + 1) contributors sums the
+  // pieces in warp order and writes C.
+  static __device__ __forceinline__ void finish_split(const MergeArgs &a, int r, int lane) {
+    const int rb = __ldg(a.rowptr + r), re = __ldg(a.rowptr + r + 1);
+    const int w1 = (int)(((long long)rb + r) / a.D);
+    const int w2 = (int)(((long long)re + r) / a.D);
+    __threadfence();
+    __syncwarp();
+    int old = 0;
+    if (lane == 0) old = atomicAdd(a.counters + w1, 1);
+    old = __shfl_sync(0xffffffffu, old, 0);
+    if (old != w2 - w1) return;
+    __threadfence();
+    if (lane < LPR) {
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int chunk = c * LPR + lane;
+        if (chunk >= a.nvec) continue;
+        float sum[VEC], x[VEC];
+        // tail piece of w1, middle pieces (tail slots), head piece of w2
+        load_vec_cg<VEC>(a.partials + (size_t)(2 * w1 + 1) * a.ldp + (size_t)chunk * VEC, sum);
+        for (int w = w1 + 1; w < w2; ++w) {
+          load_vec_cg<VEC>(a.partials + (size_t)(2 * w + 1) * a.ldp + (size_t)chunk * VEC, x);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) sum[q] += x[q];
+        }
+        load_vec_cg<VEC>(a.partials + (size_t)(2 * w2) * a.ldp + (size_t)chunk * VEC, x);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) sum[q] += x[q];
+        store_vec<VEC, true>(a.C + (size_t)r * a.F + (size_t)chunk * VEC, sum);
+      }
+    }
+    if (lane == 0) a.counters[w1] = 0;
+  }
+
+  static __device__ void run(const MergeArgs &a) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (warp >= a.P) return;
+    const long long total = (long long)a.nrows + a.nnz;
+    const long long d0 = min((long long)warp * a.D, total);
+    const long long d1 = min((long long)(warp + 1) * a.D, total);
+    if (d0 >= d1) return;
+    const int i0 = merge_search(a.rowptr, a.nrows, a.nnz, d0);
+    const int i1 = merge_search(a.rowptr, a.nrows, a.nnz, d1);
+    int j = (int)(d0 - i0);
+    const int j1 = (int)(d1 - i1);
+
+    float acc[CH][VEC];
+    for (int r = i0; r < i1; ++r) {
+      const int rb = __ldg(a.rowptr + r), re = __ldg(a.rowptr + r + 1);
+      accumulate(a, j, re, lane, acc);
+      if (j == rb) {
+        write_row<true>(a, a.C + (size_t)r * a.F, lane, acc);
+      } else {  // head piece: the row started in an earlier warp
+        write_row<false>(a, a.partials + (size_t)(2 * warp) * a.ldp, lane, acc);
+        finish_split(a, r, lane);
+      }
+      j = re;
+    }
+    if (j < j1) {  // tail (or middle) piece of row i1: continues past d1
+      accumulate(a, j, j1, lane, acc);
+      write_row<false>(a, a.partials + (size_t)(2 * warp + 1) * a.ldp, lane, acc);
+      finish_split(a, i1, lane);
+    }
+  }
+};
+
+template <int DT, int VEC, int LPR, int CH, int U>
+__global__ void __launch_bounds__(256) k_csr_spmm_merge(MergeArgs a) {
+  MergeKernel<DT, VEC, LPR, CH, U>::run(a);
+}
+
+// ---------------------------------------------------------------------------
+// host side: variant selection, grid sizing, workspace layout
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kThreads = 256;
+constexpr long long kMinEventsPerWarp = 256;
+
+struct Variant {
+  const void *fn;
+  int vec, lpr, ch;
+};
+
+template <int DT, int VEC, int LPR, int CH>
+Variant mk() {
+  constexpr int UCAP = (CH >= 8) ? 1 : (8 / CH);
+  constexpr int U = UCAP < LPR ? UCAP : LPR;
+  return Variant{(const void *)&k_csr_spmm_merge<DT, VEC, LPR, CH, U>, VEC, LPR, CH};
+}
+
+template <int DT, int VEC>
+bool pick_lpr_ch(int nvec, Variant *v) {
+  if (nvec <= 1) { *v = mk<DT, VEC, 1, 1>(); return true; }
+  if (nvec <= 2) { *v = mk<DT, VEC, 2, 1>(); return true; }
+  if (nvec <= 4) { *v = mk<DT, VEC, 4, 1>(); return true; }
+  if (nvec <= 8) { *v = mk<DT, VEC, 8, 1>(); return true; }
+  if (nvec <= 16) { *v = mk<DT, VEC, 16, 1>(); return true; }
+  if (nvec <= 32) { *v = mk<DT, VEC, 32, 1>(); return true; }
+  if (nvec <= 64) { *v = mk<DT, VEC, 32, 2>(); return true; }
+  if (nvec <= 128) { *v = mk<DT, VEC, 32, 4>(); return true; }
+  if (nvec <= 256) { *v = mk<DT, VEC, 32, 8>(); return true; }
+  if constexpr (VEC == 1) {
+    if (nvec <= 512) { *v = mk<DT, VEC, 32, 16>(); return true; }
+    if (nvec <= 1024) { *v = mk<DT, VEC, 32, 32>(); return true; }
+  }
+  return false;
+}
+
+}  // namespace
+
+gbs_status spmm_select(int dt, int F, bool aligned16, SpmmVariant *out) {
+  Variant v{};
+  bool ok = false;
+  if (dt == DT_F32) {
+    if (F % 4 == 0 && aligned16) ok = pick_lpr_ch<DT_F32, 4>(F / 4, &v);
+    else ok = pick_lpr_ch<DT_F32, 1>(F, &v);
+    if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: FP32 features need F <= 1024");
+  } else {
+    if (F % 8 != 0 || !aligned16)
+      return fail(GBS_ERR_UNSUPPORTED,
+                  "csr spmm: 16-bit features need F % 8 == 0 and 16-byte aligned B/C");
+    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(F / 8, &v) : pick_lpr_ch<DT_F16, 8>(F / 8, &v);
+    if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: 16-bit features need F <= 2048");
+  }
+  out->fn = v.fn;
+  out->vec = v.vec;
+  out->lpr = v.lpr;
+  out->ch = v.ch;
+  return GBS_OK;
+}
+
+// Number of warps (P) the launch uses: one resident wave of the variant, but
+// no warp with fewer than kMinEventsPerWarp merge events.
+gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out) {
+  static std::mutex mu;
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  int blocks_per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, v.fn, kThreads, 0));
+  }
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  const long long pmax = (long long)di.sm_count * blocks_per_sm * (kThreads / 32);
+  const long long total = (long long)nrows + nnz;
+  long long p = (total + kMinEventsPerWarp - 1) / kMinEventsPerWarp;
+  if (p > pmax) p = pmax;
+  if (p < 1) p = 1;
+  *P_out = (int)p;
+  return GBS_OK;
+}
+
+size_t spmm_workspace_bytes(int P, int F) {
+  const size_t ldp = align_up((size_t)F, 4);
+  return align_up((size_t)2 * P * ldp * sizeof(float), 256) + align_up((size_t)P * sizeof(int), 256);
+}
+
+gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
+                       const int *colind, const float *vals, const void *B, int F, float *C,
+                       void *ws, cudaStream_t stream) {
+  MergeArgs a;
+  a.nrows = nrows;
+  a.nnz = nnz;
+  a.F = F;
+  a.nvec = F / v.vec;
+  a.rowptr = rowptr;
+  a.colind = colind;
+  a.vals = vals;
+  a.B = B;
+  a.C = C;
+  a.ldp = (int)align_up((size_t)F, 4);
+  a.P = P;
+  const long long total = (long long)nrows + nnz;
+  a.D = (total + P - 1) / P;
+  if (a.D < 1) a.D = 1;
+  a.partials = reinterpret_cast<float *>(ws);
+  a.counters = reinterpret_cast<int *>(reinterpret_cast<char *>(ws) +
+                                       align_up((size_t)2 * P * a.ldp * sizeof(float), 256));
+  const int blocks = (P * 32 + kThreads - 1) / kThreads;
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(kThreads), args, 0, stream));
+  return GBS_OK;
+}
+
+gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                           const void *B, int F, const float *C) {
+  GBS_REQUIRE(nrows >= 0 && ncols >= 0 && nnz >= 0, "csr spmm: negative size");
+  GBS_REQUIRE(F >= 1, "csr spmm: F must be >= 1");
+  GBS_REQUIRE(nnz == 0 || ncols > 0, "csr spmm: nnz > 0 with ncols == 0");
+  if (nrows > 0) {
+    GBS_REQUIRE(rowptr != nullptr && C != nullptr, "csr spmm: null rowptr or C");
+  }
+  if (nnz > 0) {
+    GBS_REQUIRE(colind != nullptr && B != nullptr, "csr spmm: null colind or B");
+  }
+  return GBS_OK;
+}
+
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+gbs_status spmm_prepare(int dt, int nrows, int nnz, int F, const void *B, const float *C,
+                        SpmmVariant *v, int *P) {
+  const bool al = aligned16(B) && aligned16(C);
+  GBS_TRY(spmm_select(dt, F, al, v));
+  GBS_TRY(spmm_warps(*v, nrows, nnz, P));
+  return GBS_OK;
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+static int to_dt(gbs_dtype t) { return t == GBS_F32 ? DT_F32 : (t == GBS_BF16 ? DT_BF16 : DT_F16); }
+
+extern "C" gbs_status gbs_csr_spmm_workspace_size(int nrows, int nnz, int F, gbs_dtype btype,
+                                                  size_t *bytes) {
+  clear_error();
+  GBS_REQUIRE(bytes != nullptr, "workspace_size: null output");
+  GBS_REQUIRE(nrows >= 0 && nnz >= 0 && F >= 1, "workspace_size: bad sizes");
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "workspace_size: bad dtype");
+  // Size for the aligned variant; the unaligned FP32 fallback never needs more
+  // warps than a resident wave, and the larger of the two is returned.
+  SpmmVariant v1, v2;
+  int P1 = 1, P2 = 1;
+  gbs_status s = spmm_select(to_dt(btype), F, true, &v1);
+  if (s != GBS_OK) return s;
+  GBS_TRY(spmm_warps(v1, nrows, nnz, &P1));
+  if (btype == GBS_F32) {
+    GBS_TRY(spmm_select(DT_F32, F, false, &v2));
+    GBS_TRY(spmm_warps(v2, nrows, nnz, &P2));
+  }
+  *bytes = spmm_workspace_bytes(P1 > P2 ? P1 : P2, F);
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_csr_spmm_workspace_init(void *ws, size_t bytes, gbs_stream_t stream) {
+  clear_error();
+  if (bytes == 0) return GBS_OK;
+  GBS_REQUIRE(ws != nullptr, "workspace_init: null workspace");
+  GBS_CUDA_TRY(cudaMemsetAsync(ws, 0, bytes, (cudaStream_t)stream));
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_csr_spmm(int nrows, int ncols, int nnz, const int *rowptr,
+                                   const int *colind, const float *vals, const void *B,
+                                   gbs_dtype btype, int F, float *C, void *ws, size_t ws_bytes,
+                                   gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "csr spmm: bad dtype");
+  GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
+  if (nrows == 0) return GBS_OK;
+  SpmmVariant v;
+  int P = 0;
+  GBS_TRY(spmm_prepare(to_dt(btype), nrows, nnz, F, B, C, &v, &P));
+  const size_t need = spmm_workspace_bytes(P, F);
+  GBS_REQUIRE(ws != nullptr && ws_bytes >= need, "csr spmm: workspace missing or too small");
+  GBS_TRY(spmm_launch(v, P, nrows, nnz, rowptr, colind, vals, B, F, C, ws, (cudaStream_t)stream));
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz, const int *rowptr,
+                                       const int *colind, const float *vals, const float *B, int F,
+                                       float *C, gbs_stream_t stream) {
+  clear_error();
+  GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
+  if (nrows == 0) return GBS_OK;
+  SpmmVariant v;
+  int P = 0;
+  GBS_TRY(spmm_prepare(DT_F32, nrows, nnz, F, B, C, &v, &P));
+  const size_t need = spmm_workspace_bytes(P, F);
+  cudaStream_t s = (cudaStream_t)stream;
+  void *ws = nullptr;
+  GBS_CUDA_TRY(cudaMallocAsync(&ws, need, s));
+  cudaError_t e = cudaMemsetAsync(ws, 0, need, s);
+  gbs_status st = GBS_OK;
+  if (e != cudaSuccess) st = cuda_fail(e, "cudaMemsetAsync");
+  if (st == GBS_OK) st = spmm_launch(v, P, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
+  cudaError_t e2 = cudaFreeAsync(ws, s);
+  if (st == GBS_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaFreeAsync");
+  return st;
+}

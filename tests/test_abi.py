@@ -1,0 +1,57 @@
+"""CPU tests of the C ABI: the library loads, exports exactly what
+include/gbspmm.h declares, and rejects bad arguments on the host (no GPU
+work is issued by any call here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from spmm_eval_gb300 import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "gbspmm.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"GBS_API\s+[^;(]*?\b(gbs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "gbs_csr_spmm" in syms and "gbs_last_error" in syms
+    assert len(syms) >= 6
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(str(built_lib))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_python_binding_covers_header(built_lib):
+    assert set(declared_symbols()) == set(_lib.SIGNATURES), (
+        set(declared_symbols()) ^ set(_lib.SIGNATURES))
+
+
+def test_abi_version(built_lib):
+    assert _lib.load().gbs_abi_version() == 1
+
+
+@pytest.mark.parametrize("args, frag", [
+    ((-1, 4, 0, None, None, None, None, _lib.GBS_F32, 8, None, None, 0, None), "negative"),
+    ((4, 4, 0, None, None, None, None, _lib.GBS_F32, 0, None, None, 0, None), "F must be"),
+    ((4, 0, 5, 1, 1, None, 1, _lib.GBS_F32, 8, 1, None, 0, None), "ncols == 0"),
+    ((4, 4, 5, None, 1, None, 1, _lib.GBS_F32, 8, 1, None, 0, None), "null rowptr"),
+    ((4, 4, 0, 1, None, None, None, 7, 8, 1, None, 0, None), "bad dtype"),
+])
+def test_csr_spmm_rejects_bad_args_on_host(built_lib, args, frag):
+    with pytest.raises(_lib.GbsError) as ei:
+        _lib.call("gbs_csr_spmm", *args)
+    assert ei.value.status == _lib.GBS_ERR_INVALID_ARG
+    assert frag in str(ei.value)
+
+
+def test_empty_matrix_is_a_no_op(built_lib):
+    # nrows == 0: nothing to do, no device call
+    _lib.call("gbs_csr_spmm", 0, 0, 0, None, None, None, None, _lib.GBS_F32, 8, None, None, 0, None)

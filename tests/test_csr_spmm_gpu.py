@@ -1,0 +1,164 @@
+"""GPU parity of the merge-path CSR SpMM against the FP64 CPU oracle and
+against cuSPARSE (the library the reference verifies with,
+test_spmm_full.cu:279-307).
+
+Tolerances (stated per test):
+  * FP32 features: max relative error <= 1e-5 against FP64, where the error
+    of C[i,k] is scaled by M[i,k] = sum_j |A_ij| |B_jk| (the scale of the
+    rounding bound of a sum of products; |C| itself can be ~0 by
+    cancellation).
+  * BF16 / FP16 features: the same measure against the FP64 product of the
+    *rounded* features <= 1e-5 (accumulation), and against the FP64 product
+    of the FP32 features <= 1e-2 (incl. the storage rounding).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from spmm_eval_gb300 import graphs as G
+from spmm_eval_gb300 import ops
+
+pytestmark = pytest.mark.gpu
+
+
+def dev_csr(g, dev, with_vals=True):
+    return ops.CSR(g.rowptr.to(dev), g.colind.to(dev), g.vals.to(dev) if with_vals else None,
+                   g.nrows, g.ncols)
+
+
+def check_f32(g, B, C, vals=True, tol=1e-5):
+    ref, mag = oracle.csr_spmm_f64(g.rowptr.numpy(), g.colind.numpy(),
+                                   g.vals.numpy() if vals else None, B.numpy())
+    mx, mean = oracle.rel_err(C.cpu().numpy(), ref, mag)
+    assert mx <= tol, (mx, mean)
+    return mx, mean
+
+
+def small_graph(n, m, density, seed, empty_rows=()):
+    rng = np.random.default_rng(seed)
+    mask = rng.random((n, m)) < density
+    for r in empty_rows:
+        mask[r] = False
+    rows, cols = np.nonzero(mask)
+    counts = np.bincount(rows, minlength=n)
+    rowptr = np.zeros(n + 1, np.int32)
+    rowptr[1:] = np.cumsum(counts)
+    vals = rng.uniform(-1, 1, rows.size).astype(np.float32)
+    return G.Graph(torch.from_numpy(rowptr), torch.from_numpy(cols.astype(np.int32)),
+                   torch.from_numpy(vals), n, m)
+
+
+def test_uniform_4096x16_f32(cuda):
+    """4096 x 4096, 16 distinct uniform columns per row, B 4096 x 32 N(0,1)."""
+    g = G.uniform_rows(4096, 16)
+    B = G.normal(0x5EED + 1, 3, (4096, 32))
+    C = ops.csr_spmm(dev_csr(g, cuda), B.to(cuda))
+    check_f32(g, B, C)
+
+
+def test_matches_cusparse(cuda):
+    """Agreement with cusparseSpMM (reached through torch's CSR matmul)."""
+    g = G.uniform_rows(4096, 16)
+    B = G.normal(7, 3, (4096, 64)).to(cuda)
+    A = torch.sparse_csr_tensor(g.rowptr.long(), g.colind.long(), g.vals, (4096, 4096)).to(cuda)
+    ref = (A @ B).float()
+    C = ops.csr_spmm(dev_csr(g, cuda), B)
+    scale = (torch.sparse_csr_tensor(g.rowptr.long(), g.colind.long(), g.vals.abs(),
+                                     (4096, 4096)).to(cuda) @ B.abs())
+    rel = ((C - ref).abs() / scale.clamp_min(1e-30)).max().item()
+    assert rel <= 2e-6, rel
+
+
+@pytest.mark.parametrize("F", [1, 3, 4, 8, 16, 24, 32, 40, 64, 100, 128, 256, 512, 1024])
+def test_feature_widths_f32(cuda, F):
+    g = small_graph(300, 257, 0.05, F, empty_rows=(0, 17, 299))
+    B = G.normal(F, 1, (257, F))
+    C = ops.csr_spmm(dev_csr(g, cuda), B.to(cuda))
+    check_f32(g, B, C)
+
+
+def test_binary_values_null(cuda):
+    g = small_graph(200, 200, 0.1, 5)
+    B = G.normal(5, 1, (200, 64))
+    C = ops.csr_spmm(dev_csr(g, cuda, with_vals=False), B.to(cuda))
+    check_f32(g, B, C, vals=False)
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("F", [8, 32, 64, 256, 1024, 2048])
+def test_half_features(cuda, dtype, F):
+    g = small_graph(257, 300, 0.04, F + 1)
+    B32 = G.normal(F, 2, (300, F))
+    Bh = B32.to(dtype)
+    C = ops.csr_spmm(dev_csr(g, cuda), Bh.to(cuda))
+    # accumulation error alone (against the rounded features)
+    check_f32(g, Bh.float(), C, tol=1e-5)
+    # total error including storage rounding
+    check_f32(g, B32, C, tol=1e-2)
+
+
+def test_power_law_rows_split_across_warps(cuda):
+    """flickr-shaped graph: hub rows are cut by merge-path boundaries."""
+    g = G.flickr_like()
+    for F in (32, 64, 128, 256):
+        B = G.normal(F, 4, (g.ncols, F))
+        C = ops.csr_spmm(dev_csr(g, cuda), B.to(cuda))
+        check_f32(g, B, C)
+
+
+def test_one_long_row_many_warps(cuda):
+    """A single row holding every nonzero spans every warp's share."""
+    n, m, deg = 3, 5000, 4999
+    rowptr = torch.tensor([0, 0, deg, deg], dtype=torch.int32)
+    colind = torch.arange(deg, dtype=torch.int32)
+    vals = torch.ones(deg)
+    g = G.Graph(rowptr, colind, vals, n, m)
+    B = G.normal(11, 1, (m, 64))
+    C = ops.csr_spmm(dev_csr(g, cuda), B.to(cuda))
+    check_f32(g, B, C)
+    assert torch.all(C[0] == 0) and torch.all(C[2] == 0)
+
+
+def test_no_nonzeros_writes_zeros(cuda):
+    g = G.Graph(torch.zeros(6, dtype=torch.int32), torch.zeros(0, dtype=torch.int32),
+                torch.zeros(0), 5, 4)
+    out = torch.full((5, 16), 7.0, device=cuda)
+    ops.csr_spmm(dev_csr(g, cuda), torch.zeros(4, 16, device=cuda), out=out)
+    assert torch.all(out == 0)
+
+
+def test_deterministic_and_workspace_left_zero(cuda):
+    """Two calls on one workspace and one on a fresh zero workspace agree
+    bitwise: the arrival counters are back to zero after every call."""
+    g = G.flickr_like()
+    B = G.normal(3, 4, (g.ncols, 128)).to(cuda)
+    ws = ops.SpmmWorkspace()
+    A = dev_csr(g, cuda)
+    c1 = ops.csr_spmm(A, B, workspace=ws).clone()
+    c2 = ops.csr_spmm(A, B, workspace=ws).clone()
+    c3 = ops.csr_spmm(A, B, workspace=ops.SpmmWorkspace())
+    assert torch.equal(c1, c2) and torch.equal(c1, c3)
+
+
+def test_reddit_scale_properties(cuda):
+    """Full-size power-law graph (232,965 nodes, ~114.6M edges, F = 256):
+    linearity in B and an FP64 check on sampled rows incl. the largest hubs."""
+    g = G.reddit_like(device=cuda)
+    g = G.gcn_normalize(g)
+    A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
+    B1 = G.normal(1, 5, (g.ncols, 256), device=cuda)
+    B2 = G.normal(2, 5, (g.ncols, 256), device=cuda)
+    C1 = ops.csr_spmm(A, B1)
+    C2 = ops.csr_spmm(A, B2)
+    C12 = ops.csr_spmm(A, B1 + B2)
+    scale = ops.csr_spmm(ops.CSR(g.rowptr, g.colind, g.vals.abs(), g.nrows, g.ncols),
+                         B1.abs() + B2.abs())
+    lin = ((C12 - (C1 + C2)).abs() / scale.clamp_min(1e-30)).max().item()
+    assert lin <= 1e-5, lin
+    deg = (g.rowptr[1:] - g.rowptr[:-1]).cpu()
+    rows = torch.cat([torch.topk(deg, 16).indices, torch.arange(0, g.nrows, 997)]).numpy()
+    ref, mag = oracle.csr_spmm_f64(g.rowptr.cpu().numpy(), g.colind.cpu().numpy(),
+                                   g.vals.cpu().numpy(), B1.cpu().numpy(), rows=rows)
+    mx, _ = oracle.rel_err(C1.cpu().numpy()[rows], ref, mag)
+    assert mx <= 1e-5, mx
