@@ -269,15 +269,17 @@ def run_ours(args):
     def step_bf16():
         ops.csr_spmm(A, Bh, out=Ch, workspace=ws)
 
-    def timed(fn, steps):
+    def timed(fn, steps, tag):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(steps)]
+        torch.cuda.nvtx.range_push(tag)
         for s, e in evs:
             flush.zero_()
             s.record(stream)
             fn()
             e.record(stream)
         torch.cuda.synchronize(dev)
+        torch.cuda.nvtx.range_pop()
         return [s.elapsed_time(e) for s, e in evs]
 
     for _ in range(max(3, args.warmup)):
@@ -289,14 +291,14 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     with ClockSampler(dev.index if dev.index is not None else 0) as clk:
         t0 = time.perf_counter()
-        ms = timed(step_f32, args.steps)
+        ms = timed(step_f32, args.steps, "timed_f32")
         barrier(world)
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - t0
     clocks = clk.summary()
     ms_f32 = sum(ms) / len(ms)
     ms_f32 = max_over_ranks(ms_f32, world, dev)
-    ms_bf16 = sum(timed(step_bf16, args.steps)) / args.steps
+    ms_bf16 = sum(timed(step_bf16, args.steps, "timed_bf16")) / args.steps
 
     bytes_f32 = gather_bytes(n, nnz, F, 4)
     bytes_bf16 = gather_bytes(n, nnz, F, 2)
@@ -333,7 +335,7 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize(dev)
     e2e_steps = max(3, min(args.steps, 10))
-    ms_e2e = sum(timed(e2e_step, e2e_steps)) / e2e_steps
+    ms_e2e = sum(timed(e2e_step, e2e_steps, "timed_e2e")) / e2e_steps
     ms_e2e = max_over_ranks(ms_e2e, world, dev)
     h2d = (h_rowptr.numel() * 4 + h_colind.numel() * 4 + h_vals.numel() * 4 + h_B.numel() * 4)
     d2h = h_C.numel() * 4
@@ -376,14 +378,51 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """Small fixed launch sequence for ncu: generate, free the generator's
+    cached memory, 2 warm-up launches, then `--steps` launches of the FP32
+    SpMM (and the same of BF16).  `full` is the bench graph; `eighth` keeps
+    the 232,965 nodes (B stays larger than L2) with 1/8 of the degree."""
+    import torch
+    from spmm_eval_gb300 import graphs as G
+    from spmm_eval_gb300 import ops
+    dev = torch.device("cuda:0")
+    if args.profile_case == "full":
+        g = G.gcn_normalize(G.reddit_like(device=dev))
+    else:
+        g = G.gcn_normalize(G.chung_lu(232_965, 1.8, 59.9 / 8, 20_000.0 / 8, 0x5EED + 4, dev,
+                                       "reddit_like_eighth"))
+    B = G.normal(0x5EED + 4, 9, (g.ncols, 256), device=dev)
+    Bh = B.to(torch.bfloat16)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
+    C = torch.empty((g.nrows, 256), device=dev)
+    ws = ops.SpmmWorkspace()
+    for _ in range(2):
+        ops.csr_spmm(A, B, out=C, workspace=ws)
+    for _ in range(args.steps):
+        ops.csr_spmm(A, B, out=C, workspace=ws)
+    for _ in range(args.steps):
+        ops.csr_spmm(A, Bh, out=C, workspace=ws)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": args.profile_case, "nodes": g.nrows, "nnz": g.nnz,
+                      "device_bytes": torch.cuda.max_memory_allocated()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["full", "eighth"], default=None,
+                    help="run a short fixed launch sequence for ncu instead of the bench")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

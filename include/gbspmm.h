@@ -70,8 +70,8 @@ GBS_API int gbs_abi_version(void);
  * B may be FP32, BF16 or FP16 (btype); accumulation and C are FP32.
  * ------------------------------------------------------------------------ */
 
-/* Bytes of workspace gbs_csr_spmm needs for this shape on the current
- * device.  The workspace must be zero-filled before its first use
+/* Bytes of workspace gbs_csr_spmm / gbs_csr_spmm_cb need for this shape on
+ * the current device (any alignment, any column block).  The workspace must be zero-filled before its first use
  * (gbs_csr_spmm_workspace_init); every call leaves it zero-filled again.
  * A workspace must not be used by two calls that can overlap on the GPU. */
 GBS_API gbs_status gbs_csr_spmm_workspace_size(int nrows, int nnz, int F,
@@ -84,6 +84,16 @@ GBS_API gbs_status gbs_csr_spmm(int nrows, int ncols, int nnz, const int *d_rowp
                         const void *d_B, gbs_dtype btype, int F, float *d_C,
                         void *d_workspace, size_t workspace_bytes,
                         gbs_stream_t stream);
+
+/* Same as gbs_csr_spmm with an explicit column-block width: F is processed
+ * in F / col_block launches of col_block columns each (col_block must
+ * divide F; 0 selects the width gbs_csr_spmm would use).  Smaller blocks
+ * keep the touched slice of B resident in L2 at the cost of re-reading A. */
+GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_rowptr,
+                           const int *d_colind, const float *d_vals,
+                           const void *d_B, gbs_dtype btype, int F, int col_block,
+                           float *d_C, void *d_workspace, size_t workspace_bytes,
+                           gbs_stream_t stream);
 
 /* One-call FP32 form with the argument meaning of the cuSPARSE generic
  * SpMM used by the reference (alpha = 1, beta = 0, FP32 everywhere).

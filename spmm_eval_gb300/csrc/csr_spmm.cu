@@ -27,7 +27,10 @@
 namespace gbs {
 
 struct MergeArgs {
-  int nrows, nnz, F, nvec;
+  int nrows, nnz;
+  int F;     // width of the column block handled by this launch
+  int nvec;  // F / VEC
+  long long ldb, ldc;  // row strides of B and C (elements)
   const int *rowptr;
   const int *colind;
   const float *vals;  // may be null: binary A
@@ -73,13 +76,21 @@ struct MergeKernel {
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
 
+    // indices/values of the next batch of 32 are loaded before the current
+    // batch's gathers are issued, so their latency overlaps the gathers
+    int nx_col = 0;
+    float nx_val = 0.f;
+    if (jb + lane < je) {
+      nx_col = ld_stream_i32(a.colind + jb + lane);
+      nx_val = a.vals ? ld_stream_f32(a.vals + jb + lane) : 1.f;
+    }
     for (int base = jb; base < je; base += 32) {
       const int n_valid = min(32, je - base);
-      int my_col = 0;
-      float my_val = 0.f;
-      if (lane < n_valid) {
-        my_col = ld_stream_i32(a.colind + base + lane);
-        my_val = a.vals ? ld_stream_f32(a.vals + base + lane) : 1.f;
+      const int my_col = nx_col;
+      const float my_val = nx_val;
+      if (base + 32 + lane < je) {
+        nx_col = ld_stream_i32(a.colind + base + 32 + lane);
+        nx_val = a.vals ? ld_stream_f32(a.vals + base + 32 + lane) : 1.f;
       }
       // blocked summation: each batch of 32 nonzeros is summed into a fresh
       // partial that is then added to the row total (error ~ sqrt(32) +
@@ -100,7 +111,7 @@ struct MergeKernel {
           const float v = __shfl_sync(0xffffffffu, my_val, k);
           const bool ok = k < n_valid;
           vv[u] = ok ? v : 0.f;
-          const size_t rowbase = (size_t)col * (size_t)a.F;
+          const size_t rowbase = (size_t)col * (size_t)a.ldb;
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             const int chunk = c * LPR + sl;
@@ -168,7 +179,7 @@ struct MergeKernel {
         load_vec_cg<VEC>(a.partials + (size_t)(2 * w2) * a.ldp + (size_t)chunk * VEC, x);
 #pragma unroll
         for (int q = 0; q < VEC; ++q) sum[q] += x[q];
-        store_vec<VEC, true>(a.C + (size_t)r * a.F + (size_t)chunk * VEC, sum);
+        store_vec<VEC, true>(a.C + (size_t)r * a.ldc + (size_t)chunk * VEC, sum);
       }
     }
     if (lane == 0) a.counters[w1] = 0;
@@ -192,7 +203,7 @@ struct MergeKernel {
       const int rb = __ldg(a.rowptr + r), re = __ldg(a.rowptr + r + 1);
       accumulate(a, j, re, lane, acc);
       if (j == rb) {
-        write_row<true>(a, a.C + (size_t)r * a.F, lane, acc);
+        write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
       } else {  // head piece: the row started in an earlier warp
         write_row<false>(a, a.partials + (size_t)(2 * warp) * a.ldp, lane, acc);
         finish_split(a, r, lane);
@@ -213,27 +224,22 @@ __global__ void __launch_bounds__(256) k_csr_spmm_merge(MergeArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// host side: variant selection, grid sizing, workspace layout
+// host side: variant selection, column blocking, grid sizing, workspace
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int kThreads = 256;
 constexpr long long kMinEventsPerWarp = 256;
 
-struct Variant {
-  const void *fn;
-  int vec, lpr, ch;
-};
-
 template <int DT, int VEC, int LPR, int CH>
-Variant mk() {
+SpmmVariant mk() {
   constexpr int UCAP = (CH >= 8) ? 1 : (8 / CH);
   constexpr int U = UCAP < LPR ? UCAP : LPR;
-  return Variant{(const void *)&k_csr_spmm_merge<DT, VEC, LPR, CH, U>, VEC, LPR, CH};
+  return SpmmVariant{(const void *)&k_csr_spmm_merge<DT, VEC, LPR, CH, U>, VEC, LPR, CH};
 }
 
 template <int DT, int VEC>
-bool pick_lpr_ch(int nvec, Variant *v) {
+bool pick_lpr_ch(int nvec, SpmmVariant *v) {
   if (nvec <= 1) { *v = mk<DT, VEC, 1, 1>(); return true; }
   if (nvec <= 2) { *v = mk<DT, VEC, 2, 1>(); return true; }
   if (nvec <= 4) { *v = mk<DT, VEC, 4, 1>(); return true; }
@@ -250,31 +256,30 @@ bool pick_lpr_ch(int nvec, Variant *v) {
   return false;
 }
 
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 }  // namespace
 
-gbs_status spmm_select(int dt, int F, bool aligned16, SpmmVariant *out) {
-  Variant v{};
+// Variant for a column block of width Fw.  vec16 = 16-byte vector loads are
+// allowed (aligned pointers, F a multiple of the vector width).
+gbs_status spmm_select(int dt, int Fw, bool vec16, SpmmVariant *out) {
   bool ok = false;
   if (dt == DT_F32) {
-    if (F % 4 == 0 && aligned16) ok = pick_lpr_ch<DT_F32, 4>(F / 4, &v);
-    else ok = pick_lpr_ch<DT_F32, 1>(F, &v);
+    if (vec16 && Fw % 4 == 0) ok = pick_lpr_ch<DT_F32, 4>(Fw / 4, out);
+    else ok = pick_lpr_ch<DT_F32, 1>(Fw, out);
     if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: FP32 features need F <= 1024");
   } else {
-    if (F % 8 != 0 || !aligned16)
+    if (!vec16 || Fw % 8 != 0)
       return fail(GBS_ERR_UNSUPPORTED,
                   "csr spmm: 16-bit features need F % 8 == 0 and 16-byte aligned B/C");
-    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(F / 8, &v) : pick_lpr_ch<DT_F16, 8>(F / 8, &v);
+    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(Fw / 8, out) : pick_lpr_ch<DT_F16, 8>(Fw / 8, out);
     if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: 16-bit features need F <= 2048");
   }
-  out->fn = v.fn;
-  out->vec = v.vec;
-  out->lpr = v.lpr;
-  out->ch = v.ch;
   return GBS_OK;
 }
 
-// Number of warps (P) the launch uses: one resident wave of the variant, but
-// no warp with fewer than kMinEventsPerWarp merge events.
+// Number of warps (P): one resident wave of the variant, but no warp with
+// fewer than kMinEventsPerWarp merge events.
 gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out) {
   static std::mutex mu;
   DeviceInfo di;
@@ -294,25 +299,54 @@ gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out) {
   return GBS_OK;
 }
 
-size_t spmm_workspace_bytes(int P, int F) {
-  const size_t ldp = align_up((size_t)F, 4);
+size_t spmm_workspace_bytes(int P, int Fw) {
+  const size_t ldp = align_up((size_t)Fw, 4);
   return align_up((size_t)2 * P * ldp * sizeof(float), 256) + align_up((size_t)P * sizeof(int), 256);
 }
 
+// Column-block width.  The gathers of one launch touch ncols x Fw feature
+// elements; when B is much larger than L2 the rows of B evicted between
+// reuses dominate DRAM traffic, so F is cut into equal blocks whose slice of
+// B fits in half of L2 (A is re-streamed once per block).  col_block > 0
+// forces a width (it must divide F and keep the vector alignment).
+gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col_block, int *Fw) {
+  const int vec = !vec16 ? 1 : (dt == DT_F32 ? 4 : 8);
+  if (col_block > 0) {
+    GBS_REQUIRE(col_block <= F && F % col_block == 0, "csr spmm: col_block must divide F");
+    GBS_REQUIRE(col_block % vec == 0 || !vec16,
+                "csr spmm: col_block must be a multiple of the 16-byte vector width");
+    *Fw = col_block;
+    return GBS_OK;
+  }
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  const double esize = dt == DT_F32 ? 4.0 : 2.0;
+  const double budget = 0.5 * (double)di.l2_bytes;
+  int w = F;
+  // only worth it when rows of B are reused several times
+  if ((double)nnz < 4.0 * (double)ncols) { *Fw = F; return GBS_OK; }
+  while ((double)ncols * w * esize > budget && w % 2 == 0 && (w / 2) % vec == 0 && w / 2 >= 32)
+    w /= 2;
+  *Fw = w;
+  return GBS_OK;
+}
+
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
-                       const int *colind, const float *vals, const void *B, int F, float *C,
-                       void *ws, cudaStream_t stream) {
+                       const int *colind, const float *vals, const void *B, long long ldb, int Fw,
+                       float *C, long long ldc, void *ws, cudaStream_t stream) {
   MergeArgs a;
   a.nrows = nrows;
   a.nnz = nnz;
-  a.F = F;
-  a.nvec = F / v.vec;
+  a.F = Fw;
+  a.nvec = Fw / v.vec;
+  a.ldb = ldb;
+  a.ldc = ldc;
   a.rowptr = rowptr;
   a.colind = colind;
   a.vals = vals;
   a.B = B;
   a.C = C;
-  a.ldp = (int)align_up((size_t)F, 4);
+  a.ldp = (int)align_up((size_t)Fw, 4);
   a.P = P;
   const long long total = (long long)nrows + nnz;
   a.D = (total + P - 1) / P;
@@ -340,13 +374,47 @@ gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, con
   return GBS_OK;
 }
 
-static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B, const float *C,
+                     int col_block, SpmmPlan *p) {
+  const int vec = dt == DT_F32 ? 4 : 8;
+  p->vec16 = aligned16(B) && aligned16(C) && F % vec == 0;
+  GBS_TRY(spmm_col_block(dt, ncols, nnz, F, p->vec16, col_block, &p->Fw));
+  GBS_TRY(spmm_select(dt, p->Fw, p->vec16, &p->v));
+  GBS_TRY(spmm_warps(p->v, nrows, nnz, &p->P));
+  p->nblk = F / p->Fw;
+  p->esize = dt == DT_F32 ? 4 : 2;
+  p->ws_bytes = spmm_workspace_bytes(p->P, p->Fw);
+  return GBS_OK;
+}
 
-gbs_status spmm_prepare(int dt, int nrows, int nnz, int F, const void *B, const float *C,
-                        SpmmVariant *v, int *P) {
-  const bool al = aligned16(B) && aligned16(C);
-  GBS_TRY(spmm_select(dt, F, al, v));
-  GBS_TRY(spmm_warps(*v, nrows, nnz, P));
+// Workspace that covers every plan gbs_csr_spmm can choose for this shape
+// (any alignment, any forced column block).
+gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes) {
+  size_t best = 256;
+  for (int vec16 = 0; vec16 < 2; ++vec16) {
+    if (dt != DT_F32 && !vec16) continue;
+    for (int Fw = 1; Fw <= F; ++Fw) {
+      if (F % Fw != 0) continue;
+      SpmmVariant v;
+      if (spmm_select(dt, Fw, vec16 != 0, &v) != GBS_OK) { clear_error(); continue; }
+      int P = 1;
+      GBS_TRY(spmm_warps(v, nrows, nnz, &P));
+      size_t b = spmm_workspace_bytes(P, Fw);
+      if (b > best) best = b;
+    }
+  }
+  *bytes = best;
+  return GBS_OK;
+}
+
+gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
+                    const float *vals, const void *B, int F, float *C, void *ws,
+                    cudaStream_t stream) {
+  for (int b = 0; b < p.nblk; ++b) {
+    const char *Bb = reinterpret_cast<const char *>(B) + (size_t)b * p.Fw * p.esize;
+    GBS_TRY(spmm_launch(p.v, p.P, nrows, nnz, rowptr, colind, vals, Bb, F, p.Fw,
+                        C + (size_t)b * p.Fw, F, ws, stream));
+  }
   return GBS_OK;
 }
 
@@ -362,19 +430,7 @@ extern "C" gbs_status gbs_csr_spmm_workspace_size(int nrows, int nnz, int F, gbs
   GBS_REQUIRE(bytes != nullptr, "workspace_size: null output");
   GBS_REQUIRE(nrows >= 0 && nnz >= 0 && F >= 1, "workspace_size: bad sizes");
   GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "workspace_size: bad dtype");
-  // Size for the aligned variant; the unaligned FP32 fallback never needs more
-  // warps than a resident wave, and the larger of the two is returned.
-  SpmmVariant v1, v2;
-  int P1 = 1, P2 = 1;
-  gbs_status s = spmm_select(to_dt(btype), F, true, &v1);
-  if (s != GBS_OK) return s;
-  GBS_TRY(spmm_warps(v1, nrows, nnz, &P1));
-  if (btype == GBS_F32) {
-    GBS_TRY(spmm_select(DT_F32, F, false, &v2));
-    GBS_TRY(spmm_warps(v2, nrows, nnz, &P2));
-  }
-  *bytes = spmm_workspace_bytes(P1 > P2 ? P1 : P2, F);
-  return GBS_OK;
+  return spmm_workspace_upper(to_dt(btype), nrows, nnz, F, bytes);
 }
 
 extern "C" gbs_status gbs_csr_spmm_workspace_init(void *ws, size_t bytes, gbs_stream_t stream) {
@@ -385,21 +441,34 @@ extern "C" gbs_status gbs_csr_spmm_workspace_init(void *ws, size_t bytes, gbs_st
   return GBS_OK;
 }
 
+static gbs_status csr_spmm_impl(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                                const float *vals, const void *B, gbs_dtype btype, int F, float *C,
+                                int col_block, void *ws, size_t ws_bytes, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "csr spmm: bad dtype");
+  GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
+  GBS_REQUIRE(col_block >= 0, "csr spmm: negative col_block");
+  if (nrows == 0) return GBS_OK;
+  SpmmPlan p;
+  GBS_TRY(spmm_plan(to_dt(btype), nrows, ncols, nnz, F, B, C, col_block, &p));
+  GBS_REQUIRE(ws != nullptr && ws_bytes >= p.ws_bytes, "csr spmm: workspace missing or too small");
+  return spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws, (cudaStream_t)stream);
+}
+
 extern "C" gbs_status gbs_csr_spmm(int nrows, int ncols, int nnz, const int *rowptr,
                                    const int *colind, const float *vals, const void *B,
                                    gbs_dtype btype, int F, float *C, void *ws, size_t ws_bytes,
                                    gbs_stream_t stream) {
-  clear_error();
-  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "csr spmm: bad dtype");
-  GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
-  if (nrows == 0) return GBS_OK;
-  SpmmVariant v;
-  int P = 0;
-  GBS_TRY(spmm_prepare(to_dt(btype), nrows, nnz, F, B, C, &v, &P));
-  const size_t need = spmm_workspace_bytes(P, F);
-  GBS_REQUIRE(ws != nullptr && ws_bytes >= need, "csr spmm: workspace missing or too small");
-  GBS_TRY(spmm_launch(v, P, nrows, nnz, rowptr, colind, vals, B, F, C, ws, (cudaStream_t)stream));
-  return GBS_OK;
+  return csr_spmm_impl(nrows, ncols, nnz, rowptr, colind, vals, B, btype, F, C, 0, ws, ws_bytes,
+                       stream);
+}
+
+extern "C" gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *rowptr,
+                                      const int *colind, const float *vals, const void *B,
+                                      gbs_dtype btype, int F, int col_block, float *C, void *ws,
+                                      size_t ws_bytes, gbs_stream_t stream) {
+  return csr_spmm_impl(nrows, ncols, nnz, rowptr, colind, vals, B, btype, F, C, col_block, ws,
+                       ws_bytes, stream);
 }
 
 extern "C" gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz, const int *rowptr,
@@ -408,17 +477,15 @@ extern "C" gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz, const int 
   clear_error();
   GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
   if (nrows == 0) return GBS_OK;
-  SpmmVariant v;
-  int P = 0;
-  GBS_TRY(spmm_prepare(DT_F32, nrows, nnz, F, B, C, &v, &P));
-  const size_t need = spmm_workspace_bytes(P, F);
+  SpmmPlan p;
+  GBS_TRY(spmm_plan(DT_F32, nrows, ncols, nnz, F, B, C, 0, &p));
   cudaStream_t s = (cudaStream_t)stream;
   void *ws = nullptr;
-  GBS_CUDA_TRY(cudaMallocAsync(&ws, need, s));
-  cudaError_t e = cudaMemsetAsync(ws, 0, need, s);
+  GBS_CUDA_TRY(cudaMallocAsync(&ws, p.ws_bytes, s));
+  cudaError_t e = cudaMemsetAsync(ws, 0, p.ws_bytes, s);
   gbs_status st = GBS_OK;
   if (e != cudaSuccess) st = cuda_fail(e, "cudaMemsetAsync");
-  if (st == GBS_OK) st = spmm_launch(v, P, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
+  if (st == GBS_OK) st = spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
   cudaError_t e2 = cudaFreeAsync(ws, s);
   if (st == GBS_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaFreeAsync");
   return st;

@@ -11,15 +11,29 @@ struct SpmmVariant {
   int vec, lpr, ch;
 };
 
-gbs_status spmm_select(int dt, int F, bool aligned16, SpmmVariant *out);
+struct SpmmPlan {
+  SpmmVariant v;
+  bool vec16;
+  int Fw;    // column-block width
+  int nblk;  // F / Fw launches
+  int P;     // warps per launch
+  int esize; // bytes per B element
+  size_t ws_bytes;
+};
+
+gbs_status spmm_select(int dt, int Fw, bool vec16, SpmmVariant *out);
 gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out);
-size_t spmm_workspace_bytes(int P, int F);
+size_t spmm_workspace_bytes(int P, int Fw);
+gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes);
 gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
                            const void *B, int F, const float *C);
-gbs_status spmm_prepare(int dt, int nrows, int nnz, int F, const void *B, const float *C,
-                        SpmmVariant *v, int *P);
+gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B, const float *C,
+                     int col_block, SpmmPlan *p);
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
-                       const int *colind, const float *vals, const void *B, int F, float *C,
-                       void *ws, cudaStream_t stream);
+                       const int *colind, const float *vals, const void *B, long long ldb, int Fw,
+                       float *C, long long ldc, void *ws, cudaStream_t stream);
+gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
+                    const float *vals, const void *B, int F, float *C, void *ws,
+                    cudaStream_t stream);
 
 }  // namespace gbs

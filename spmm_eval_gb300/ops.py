@@ -75,15 +75,23 @@ class SpmmWorkspace:
         return self.buf
 
 
+_WS_CACHE: dict[tuple, int] = {}
+
+
 def spmm_workspace_bytes(nrows: int, nnz: int, F: int, dtype: torch.dtype) -> int:
-    out = C.c_size_t(0)
-    _lib.call("gbs_csr_spmm_workspace_size", nrows, nnz, F, _DT[dtype], C.byref(out))
-    return int(out.value)
+    key = (torch.cuda.current_device(), nrows, nnz, F, dtype)
+    if key not in _WS_CACHE:
+        out = C.c_size_t(0)
+        _lib.call("gbs_csr_spmm_workspace_size", nrows, nnz, F, _DT[dtype], C.byref(out))
+        _WS_CACHE[key] = int(out.value)
+    return _WS_CACHE[key]
 
 
 def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
-             workspace: SpmmWorkspace | None = None) -> torch.Tensor:
-    """C = A @ B with A in CSR, B (ncols x F) FP32/BF16/FP16, C FP32."""
+             workspace: SpmmWorkspace | None = None, col_block: int = 0) -> torch.Tensor:
+    """C = A @ B with A in CSR, B (ncols x F) FP32/BF16/FP16, C FP32.
+
+    col_block > 0 forces the column-block width (must divide F)."""
     A.validate_layout()
     _check_cuda("B", B, tuple(_DT))
     if B.dim() != 2 or B.shape[0] != A.ncols:
@@ -98,7 +106,7 @@ def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
     ws = workspace or SpmmWorkspace()
     nbytes = spmm_workspace_bytes(A.nrows, A.nnz, F, B.dtype)
     buf = ws.get(nbytes, B.device)
-    _lib.call("gbs_csr_spmm", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
-              _ptr(A.vals), _ptr(B), _DT[B.dtype], F, _ptr(out), _ptr(buf), buf.numel(),
-              _stream(B.device))
+    _lib.call("gbs_csr_spmm_cb", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
+              _ptr(A.vals), _ptr(B), _DT[B.dtype], F, int(col_block), _ptr(out), _ptr(buf),
+              buf.numel(), _stream(B.device))
     return out

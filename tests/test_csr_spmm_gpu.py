@@ -162,3 +162,21 @@ def test_reddit_scale_properties(cuda):
                                    g.vals.cpu().numpy(), B1.cpu().numpy(), rows=rows)
     mx, _ = oracle.rel_err(C1.cpu().numpy()[rows], ref, mag)
     assert mx <= 1e-5, mx
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("cb", [8, 32, 64, 128, 256])
+def test_column_blocks(cuda, dtype, cb):
+    """Forced column-block widths give the same result as one full-width
+    launch (each column is summed in the same order in both)."""
+    g = G.flickr_like()
+    B = G.normal(9, 4, (g.ncols, 256)).to(dtype)
+    A = dev_csr(g, cuda)
+    full = ops.csr_spmm(A, B.to(cuda), col_block=256)
+    if dtype == torch.bfloat16 and cb == 8:
+        cb = 16
+    part = ops.csr_spmm(A, B.to(cuda), col_block=cb)
+    check_f32(g, B.float(), part)
+    # The lane split of a row changes with the block width (sub-group count),
+    # so agreement is to rounding, not bitwise.
+    assert torch.allclose(part, full, rtol=1e-5, atol=1e-5)
