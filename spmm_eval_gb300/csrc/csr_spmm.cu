@@ -76,21 +76,13 @@ struct MergeKernel {
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
 
-    // indices/values of the next batch of 32 are loaded before the current
-    // batch's gathers are issued, so their latency overlaps the gathers
-    int nx_col = 0;
-    float nx_val = 0.f;
-    if (jb + lane < je) {
-      nx_col = ld_stream_i32(a.colind + jb + lane);
-      nx_val = a.vals ? ld_stream_f32(a.vals + jb + lane) : 1.f;
-    }
     for (int base = jb; base < je; base += 32) {
       const int n_valid = min(32, je - base);
-      const int my_col = nx_col;
-      const float my_val = nx_val;
-      if (base + 32 + lane < je) {
-        nx_col = ld_stream_i32(a.colind + base + 32 + lane);
-        nx_val = a.vals ? ld_stream_f32(a.vals + base + 32 + lane) : 1.f;
+      int my_col = 0;
+      float my_val = 0.f;
+      if (lane < n_valid) {
+        my_col = ld_stream_i32(a.colind + base + lane);
+        my_val = a.vals ? ld_stream_f32(a.vals + base + lane) : 1.f;
       }
       // blocked summation: each batch of 32 nonzeros is summed into a fresh
       // partial that is then added to the row total (error ~ sqrt(32) +
@@ -304,12 +296,16 @@ size_t spmm_workspace_bytes(int P, int Fw) {
   return align_up((size_t)2 * P * ldp * sizeof(float), 256) + align_up((size_t)P * sizeof(int), 256);
 }
 
-// Column-block width.  The gathers of one launch touch ncols x Fw feature
-// elements; when B is much larger than L2 the rows of B evicted between
-// reuses dominate DRAM traffic, so F is cut into equal blocks whose slice of
-// B fits in half of L2 (A is re-streamed once per block).  col_block > 0
-// forces a width (it must divide F and keep the vector alignment).
+// Column-block width.  col_block > 0 forces F / col_block launches of
+// col_block columns (it must divide F and keep the vector alignment); each
+// launch re-streams A but touches only its slice of B.  Measured on GB300 for
+// the 232,965-node / 114.8M-edge graph at F = 256 (B = 238 MB > L2), every
+// split was slower than one full-width launch (FP32: 8.3 ms full, 9.5 ms at
+// 128, 9.9 ms at 64; BF16 likewise), because the per-nonzero work of the
+// index stream is paid once per block; the default is therefore F.
 gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col_block, int *Fw) {
+  (void)ncols;
+  (void)nnz;
   const int vec = !vec16 ? 1 : (dt == DT_F32 ? 4 : 8);
   if (col_block > 0) {
     GBS_REQUIRE(col_block <= F && F % col_block == 0, "csr spmm: col_block must divide F");
@@ -318,16 +314,7 @@ gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col
     *Fw = col_block;
     return GBS_OK;
   }
-  DeviceInfo di;
-  GBS_TRY(device_info(&di));
-  const double esize = dt == DT_F32 ? 4.0 : 2.0;
-  const double budget = 0.5 * (double)di.l2_bytes;
-  int w = F;
-  // only worth it when rows of B are reused several times
-  if ((double)nnz < 4.0 * (double)ncols) { *Fw = F; return GBS_OK; }
-  while ((double)ncols * w * esize > budget && w % 2 == 0 && (w / 2) % vec == 0 && w / 2 >= 32)
-    w /= 2;
-  *Fw = w;
+  *Fw = F;
   return GBS_OK;
 }
 

@@ -17,6 +17,7 @@ struct Feat;
 template <>
 struct Feat<DT_F32, 4> {
   using raw = float4;
+  using storage_t = float;
   static __device__ __forceinline__ raw load(const void *base, size_t elem) {
     return ld_nc_f4(reinterpret_cast<const float *>(base) + elem);
   }
@@ -35,6 +36,7 @@ struct Feat<DT_F32, 4> {
 template <>
 struct Feat<DT_F32, 1> {
   using raw = float;
+  using storage_t = float;
   static __device__ __forceinline__ raw load(const void *base, size_t elem) {
     return __ldg(reinterpret_cast<const float *>(base) + elem);
   }
@@ -48,6 +50,7 @@ struct Feat<DT_F32, 1> {
 template <>
 struct Feat<DT_BF16, 8> {
   using raw = uint4;
+  using storage_t = uint16_t;
   static __device__ __forceinline__ raw load(const void *base, size_t elem) {
     return ld_nc_u4(reinterpret_cast<const uint16_t *>(base) + elem);
   }
@@ -71,6 +74,7 @@ struct Feat<DT_BF16, 8> {
 template <>
 struct Feat<DT_F16, 8> {
   using raw = uint4;
+  using storage_t = uint16_t;
   static __device__ __forceinline__ raw load(const void *base, size_t elem) {
     return ld_nc_u4(reinterpret_cast<const uint16_t *>(base) + elem);
   }
