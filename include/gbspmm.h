@@ -103,6 +103,24 @@ GBS_API gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz,
                             const float *d_vals, const float *d_B, int F,
                             float *d_C, gbs_stream_t stream);
 
+/* CSR SpMM that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that may not allocate while they run (a
+ * framework that reserves its device memory up front in its own pool, a
+ * serving loop that bans cudaMalloc/cudaFree because they can synchronise
+ * the device).  Same arguments and result as gbs_csr_spmm minus the
+ * workspace: the kernel's scratch is a fixed 8 MiB array compiled into the
+ * library, held on every GPU that loads the library until the process exits.
+ * Shapes whose scratch would not fit are rejected with GBS_ERR_INVALID_ARG.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture starts.  All calls share the array:
+ * calls that can overlap on the GPU race and must be serialised by the
+ * caller. */
+GBS_API gbs_status gbs_csr_spmm_noalloc(int nrows, int ncols, int nnz,
+                                const int *d_rowptr, const int *d_colind,
+                                const float *d_vals, const void *d_B,
+                                gbs_dtype btype, int F, float *d_C,
+                                gbs_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,96 @@
+// CSR SpMM that allocates nothing: the merge-path kernel of csr_spmm.cu run
+// with its scratch (split-row partial sums and arrival counters) in a
+// fixed-size array compiled into this library instead of a caller-provided
+// workspace.
+//
+// Who needs it: a caller that may not allocate device memory while it runs.
+// Typical cases are a host application or framework that reserves all of its
+// device memory up front in its own pool (an extra cudaMalloc from a library
+// would fail or fragment that pool), and latency-critical serving loops that
+// ban cudaMalloc/cudaFree on the request path because those calls can
+// synchronise the whole device.  Such a caller still owns A, B and C; only
+// the kernel's scratch comes from here.
+//
+// Costs of the fixed array: every GPU that loads the library holds
+// kNoAllocScratchBytes of device memory until the process exits, and all
+// calls share it, so two calls that can overlap on the GPU (different
+// streams, or different host threads on one device) race on it and must be
+// serialised by the caller.
+#include <mutex>
+
+#include "common.cuh"
+#include "csr_spmm.cuh"
+
+namespace gbs {
+
+// 8 MiB: enough for the partial sums of one full resident wave of warps on
+// a 152-SM GPU up to F = 1024 FP32 columns per launch; the warp count is
+// reduced when a shape would need more.
+constexpr size_t kNoAllocScratchBytes = 8u << 20;
+
+static __device__ __align__(256) unsigned char g_spmm_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+// Device address of g_spmm_scratch, looked up once per device.  In host code
+// the name g_spmm_scratch is only a host-side stand-in for the symbol; the
+// address a kernel may use comes from cudaGetSymbolAddress with that device
+// current.
+gbs_status scratch_address(void **out) {
+  static std::mutex mu;
+  static void *addr[64] = {nullptr};
+  int dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "csr spmm noalloc: device ordinal >= 64");
+  std::lock_guard<std::mutex> lock(mu);
+  if (addr[dev] == nullptr) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_spmm_scratch)");
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return GBS_OK;
+}
+
+// Largest warp count whose partial slots and counters fit in the array.
+int fit_warps(int P, int Fw) {
+  while (P > 1 && spmm_workspace_bytes(P, Fw) > kNoAllocScratchBytes) P = P * 3 / 4;
+  return P;
+}
+
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" gbs_status gbs_csr_spmm_noalloc(int nrows, int ncols, int nnz, const int *rowptr,
+                                           const int *colind, const float *vals, const void *B,
+                                           gbs_dtype btype, int F, float *C,
+                                           gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16,
+              "csr spmm noalloc: bad dtype");
+  GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, B, F, C));
+  if (nrows == 0) return GBS_OK;
+  const int dt = btype == GBS_F32 ? 0 : (btype == GBS_BF16 ? 1 : 2);
+  SpmmPlan p;
+  GBS_TRY(spmm_plan(dt, nrows, ncols, nnz, F, B, C, 0, &p));
+  p.P = fit_warps(p.P, p.Fw);
+  p.ws_bytes = spmm_workspace_bytes(p.P, p.Fw);
+  if (p.ws_bytes > kNoAllocScratchBytes)
+    return fail(GBS_ERR_INVALID_ARG,
+                "csr spmm noalloc: F = " + std::to_string(F) + " needs " +
+                    std::to_string(p.ws_bytes) + " bytes of scratch, more than the " +
+                    std::to_string(kNoAllocScratchBytes) + "-byte static array");
+  void *ws = nullptr;
+  GBS_TRY(scratch_address(&ws));
+  cudaStream_t s = (cudaStream_t)stream;
+  // The array keeps whatever the previous call left in it.  Only the arrival
+  // counters must start at zero (partial slots are written before they are
+  // read), so clear exactly that region for this call's layout.
+  const size_t counters_off = align_up((size_t)2 * p.P * align_up((size_t)p.Fw, 4) * sizeof(float), 256);
+  GBS_CUDA_TRY(cudaMemsetAsync(static_cast<char *>(ws) + counters_off, 0,
+                               (size_t)p.P * sizeof(int), s));
+  return spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
+}
