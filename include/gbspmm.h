@@ -103,6 +103,93 @@ GBS_API gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz,
                             const float *d_vals, const float *d_B, int F,
                             float *d_C, gbs_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * CSR -> B2SR packing (tile = 4, 8, 16 or 32)
+ *
+ * B2SR layout (the reference's): block-row i covers CSR rows [i*tile,
+ * (i+1)*tile); it holds one tile per distinct floor(col/tile) of those rows,
+ * ascending; tile b stores row r as a tile-bit word at element tile*b + r,
+ * column 0 in the most significant of the tile bits.  Element type: uint8
+ * (tile 4: low nibble; tile 8), uint16 (16), uint32 (32).  Every stored CSR
+ * entry sets its bit; values are ignored.
+ * ------------------------------------------------------------------------ */
+
+/* Tile counts: writes bsr_rowptr[0..mb] (mb = ceil(nrows/tile)) and returns
+ * the number of tiles in *h_nnzb.  Validates the CSR (column range, columns
+ * ascending within a row).  Synchronises the stream.  Replaces
+ * cusparseXcsr2bsrNnz in CSR2B2SR (test_spmm_full.cu:147-151). */
+GBS_API gbs_status gbs_csr2b2sr_nnzb(int nrows, int ncols, int nnz,
+                             const int *d_rowptr, const int *d_colind,
+                             int tile, int *d_bsr_rowptr, int *h_nnzb,
+                             gbs_stream_t stream);
+/* Fills bsr_colind[nnzb] and bsr_val[nnzb*tile] (bsr_rowptr from
+ * gbs_csr2b2sr_nnzb on the same CSR).  Replaces the per-block-row loop of
+ * csr2bsr_batch_{4,8,16,32} (csr2bsr_batch_bsrbmv.cu:207-397, :403-579,
+ * :654-830, :894-1070) with one kernel. */
+GBS_API gbs_status gbs_csr2b2sr(int nrows, int ncols, int nnz, const int *d_rowptr,
+                        const int *d_colind, int tile, const int *d_bsr_rowptr,
+                        int *d_bsr_colind, void *d_bsr_val, gbs_stream_t stream);
+/* Drop-in with the argument list of csr2bsr_batch_{4,8,16,32}
+ * (csr2bsr_batch_bsrbmv.cu:207): host CSR in, caller-allocated device B2SR
+ * out, nblocks as computed by cusparseXcsr2bsrNnz (checked).  Synchronous,
+ * legacy default stream; allocates device copies of the CSR internally. */
+GBS_API gbs_status gbs_csr2bsr_batch(const int *h_csrRowPtr, const int *h_csrColInd,
+                             int nrows, int ncols, int nnz, int *d_bsrRowPtr,
+                             int *d_bsrColInd, void *d_bsrVal, int blocksize,
+                             int nblockrows, int nblocks);
+
+/* "Aligned" B2SR-8/16 (packUchar2AlignedUnsigned / packUshort2Aligned-
+ * Unsigned, csr2bsr_batch_bsrbmv.cu:586-648, :837-888): tiles of a
+ * block-row padded to a multiple of 4 (tile 8) / 2 (tile 16), padded colind
+ * 0; uint32 word j of a group packs row j of its tiles, first tile in the
+ * most significant byte/half.  nnzb writes new_rowptr (padded tile counts)
+ * and returns the padded tile total (words = total*tile/g) synchronously. */
+GBS_API gbs_status gbs_b2sr_aligned_nnzb(int tile, int nblockrows,
+                                 const int *d_bsr_rowptr, int *d_new_rowptr,
+                                 int *h_ntiles, gbs_stream_t stream);
+GBS_API gbs_status gbs_b2sr_pack_aligned(int tile, int nblockrows,
+                                 const int *d_bsr_rowptr, const int *d_bsr_colind,
+                                 const void *d_bsr_val, const int *d_new_rowptr,
+                                 int *d_new_colind, uint32_t *d_new_val,
+                                 gbs_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * B2SR x dense (binary A):  C = A01 * B, C FP32 nrows x F (every row
+ * written).  Tile 4 adds in the order of spmm4_full_full_new2
+ * (spmm.cu:877-956), so its result is bitwise the reference's for any FP32
+ * B; other tiles add in column order (exact for integer-valued B).
+ * ------------------------------------------------------------------------ */
+GBS_API gbs_status gbs_b2sr_spmm(int tile, int nrows, int nblockrows,
+                         const int *d_bsr_rowptr, const int *d_bsr_colind,
+                         const void *d_bsr_val, const void *d_B, gbs_dtype btype,
+                         int F, float *d_C, gbs_stream_t stream);
+/* Drop-in for the launch of spmm4_full_full_new2 (test_spmm_full.cu:351-361,
+ * same arguments plus a stream): C must be zero-filled by the caller, only
+ * nonzero results are stored (as the reference does, spmm.cu:947-954). */
+GBS_API gbs_status gbs_spmm4_full_full(const uint8_t *A, const float *B, float *C,
+                               const int *rowptr, const int *colind,
+                               int nblockrows, int B_cols, gbs_stream_t stream);
+
+/* B2SR x packed-bit features -> int32 (BMV for F <= 32, BMM above; the
+ * reference names these kernels but does not ship them,
+ * csr2bsr_batch_bsrbmv.cu:1).  X: ceil(F/32) uint32 words per row as
+ * gbs_pack_sign_rows writes them.  C[i][k] = sum_j A_ij * bit_jk, or with
+ * signed_form != 0: 2*C01 - deg(i), the +-1 product. F <= 1024. */
+GBS_API gbs_status gbs_b2sr_bmm(int tile, int nrows, int nblockrows,
+                        const int *d_bsr_rowptr, const int *d_bsr_colind,
+                        const void *d_bsr_val, const uint32_t *d_X, int F,
+                        int signed_form, int32_t *d_C, gbs_stream_t stream);
+
+/* Dense sign packing, bit = (x >= 0), first column in bit 31, elements
+ * outside the matrix read as -1 (bit 0).
+ * rows : ToBit32RowDenseSign (spmm.cu:75-91), out[r*ceil(F/32) + w].
+ * colud: ToBit32ColUd (spmm.cu:93-111), out[w*Hp + r], Hp = 32*ceil(H/32),
+ *        the word-major layout the binary GEMM reads. */
+GBS_API gbs_status gbs_pack_sign_rows(const float *d_X, int n, int F, uint32_t *d_out,
+                              gbs_stream_t stream);
+GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t *d_out,
+                               gbs_stream_t stream);
+
 /* CSR SpMM that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not allocate while they run (a
  * framework that reserves its device memory up front in its own pool, a

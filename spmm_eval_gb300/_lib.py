@@ -41,6 +41,16 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_csr_spmm_cb": (st, [i32, i32, i32, p, p, p, p, i32, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_f32": (st, [i32, i32, i32, p, p, p, p, i32, p, p]),
     "gbs_csr_spmm_noalloc": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
+    "gbs_csr2b2sr_nnzb": (st, [i32, i32, i32, p, p, i32, p, pi32, p]),
+    "gbs_csr2b2sr": (st, [i32, i32, i32, p, p, i32, p, p, p, p]),
+    "gbs_csr2bsr_batch": (st, [p, p, i32, i32, i32, p, p, p, i32, i32, i32]),
+    "gbs_b2sr_aligned_nnzb": (st, [i32, i32, p, p, pi32, p]),
+    "gbs_b2sr_pack_aligned": (st, [i32, i32, p, p, p, p, p, p, p]),
+    "gbs_b2sr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
+    "gbs_spmm4_full_full": (st, [p, p, p, p, p, i32, i32, p]),
+    "gbs_b2sr_bmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
+    "gbs_pack_sign_rows": (st, [p, i32, i32, p, p]),
+    "gbs_pack_sign_colud": (st, [p, i32, i32, p, p]),
 }
 
 

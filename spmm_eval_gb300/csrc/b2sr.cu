@@ -1,0 +1,714 @@
+// B2SR ("binarised BSR") on sm_103a: CSR -> B2SR packing for tiles 4/8/16/32,
+// the "aligned" B2SR-8/16 variants, B2SR x dense SpMM, B2SR x packed-bit BMM
+// and the dense sign packers.
+//
+// Layout (the reference's, csr2bsr_batch_bsrbmv.cu + spmm.cu ToBit*Col):
+// block-row i covers CSR rows [i*ts, (i+1)*ts); it has one tile per distinct
+// floor(col / ts) of those rows, in ascending order; tile b stores its ts rows
+// as ts-bit words, element ts*b + r = row r, column 0 in the most significant
+// of the ts bits (uint8 for ts 4 (low nibble) and 8, uint16 for 16, uint32
+// for 32).  Any stored CSR entry sets its bit (values are ignored, as the
+// reference forces them to 1.0 before packing, csr2bsr_batch_bsrbmv.cu:296).
+#include <climits>
+#include <vector>
+
+#include "common.cuh"
+#include "feat.cuh"
+#include "util.cuh"
+
+namespace gbs {
+
+template <int TS> struct TileT;
+template <> struct TileT<4> { using T = uint8_t; };
+template <> struct TileT<8> { using T = uint8_t; };
+template <> struct TileT<16> { using T = uint16_t; };
+template <> struct TileT<32> { using T = uint32_t; };
+
+// ---------------------------------------------------------------------------
+// Packing.  A group of ts lanes owns one block-row (lane r walks CSR row
+// i*ts + r).  Each step takes the smallest tile column m at the heads of the
+// ts rows (__reduce_min_sync over the group), every lane consumes its
+// entries in that tile column and ORs their bits into its tile row; the tiles
+// therefore come out in ascending order with no sort and no atomics.
+// ---------------------------------------------------------------------------
+template <int TS, bool FILL>
+__global__ void __launch_bounds__(256)
+    k_b2sr_pack(int nrows, int ncols, int mb, const int *__restrict__ rowptr,
+                const int *__restrict__ colind, int *__restrict__ counts, const int *__restrict__ brp,
+                int *__restrict__ bcol, typename TileT<TS>::T *__restrict__ bval, int *__restrict__ err) {
+  using VT = typename TileT<TS>::T;
+  constexpr int G = 32 / TS;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / TS, r = lane % TS;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long strip = gw * G + g;
+  if (strip >= mb) return;  // the whole group leaves together
+  const unsigned gmask = (TS == 32) ? 0xffffffffu : (((1u << TS) - 1u) << (g * TS));
+  const long long row = strip * TS + r;
+  int p = 0, e = 0;
+  if (row < nrows) {
+    p = __ldg(rowptr + row);
+    e = __ldg(rowptr + row + 1);
+  }
+  const int rs = p;
+  const int out = FILL ? __ldg(brp + strip) : 0;
+  int cnt = 0, prev_m = -1;
+  while (true) {
+    int head = INT_MAX;
+    if (p < e) {
+      const int c = __ldg(colind + p);
+      if (!FILL && (c < 0 || c >= ncols || (p > rs && __ldg(colind + p - 1) > c))) {
+        atomicOr(err, 1);
+        p = e;
+      } else {
+        head = c / TS;
+      }
+    }
+    const int m = __reduce_min_sync(gmask, head);
+    if (m == INT_MAX) break;
+    if (!FILL && m < prev_m) atomicOr(err, 1);  // unreachable for sorted, in-range input
+    prev_m = m;
+    uint32_t bits = 0;
+    while (p < e) {
+      const int c = __ldg(colind + p);
+      if (c / TS != m) break;
+      if (!FILL && (c >= ncols || (p > rs && __ldg(colind + p - 1) > c))) {
+        atomicOr(err, 1);
+        p = e;
+        break;
+      }
+      bits |= 1u << (TS - 1 - (c % TS));
+      ++p;
+    }
+    if (FILL) {
+      if (r == 0) bcol[out + cnt] = m;
+      bval[(size_t)(out + cnt) * TS + r] = (VT)bits;
+    }
+    ++cnt;
+  }
+  if (!FILL && r == 0) counts[strip] = cnt;
+}
+
+template <int TS>
+gbs_status launch_pack(bool fill, int nrows, int ncols, int mb, const int *rowptr, const int *colind,
+                       int *counts, const int *brp, int *bcol, void *bval, int *err, cudaStream_t s) {
+  constexpr int G = 32 / TS;
+  const long long warps = ((long long)mb + G - 1) / G;
+  const int blocks = (int)((warps * 32 + 255) / 256);
+  using VT = typename TileT<TS>::T;
+  if (blocks == 0) return GBS_OK;
+  if (fill)
+    k_b2sr_pack<TS, true><<<blocks, 256, 0, s>>>(nrows, ncols, mb, rowptr, colind, counts, brp, bcol,
+                                                 reinterpret_cast<VT *>(bval), err);
+  else
+    k_b2sr_pack<TS, false><<<blocks, 256, 0, s>>>(nrows, ncols, mb, rowptr, colind, counts, brp, bcol,
+                                                  reinterpret_cast<VT *>(bval), err);
+  return check_launch("k_b2sr_pack");
+}
+
+gbs_status pack_dispatch(int ts, bool fill, int nrows, int ncols, int mb, const int *rowptr,
+                         const int *colind, int *counts, const int *brp, int *bcol, void *bval,
+                         int *err, cudaStream_t s) {
+  switch (ts) {
+    case 4: return launch_pack<4>(fill, nrows, ncols, mb, rowptr, colind, counts, brp, bcol, bval, err, s);
+    case 8: return launch_pack<8>(fill, nrows, ncols, mb, rowptr, colind, counts, brp, bcol, bval, err, s);
+    case 16: return launch_pack<16>(fill, nrows, ncols, mb, rowptr, colind, counts, brp, bcol, bval, err, s);
+    case 32: return launch_pack<32>(fill, nrows, ncols, mb, rowptr, colind, counts, brp, bcol, bval, err, s);
+    default: return fail(GBS_ERR_UNSUPPORTED, "b2sr: tile size must be 4, 8, 16 or 32");
+  }
+}
+
+static size_t tile_elem_bytes(int ts) { return ts <= 8 ? 1 : (ts == 16 ? 2 : 4); }
+
+// counts -> bsrRowPtr (exclusive scan, total in [mb]) and nnzb / validity to
+// the host.
+gbs_status b2sr_nnzb(int nrows, int ncols, int nnz, const int *rowptr, const int *colind, int ts,
+                     int *bsr_rowptr, int *h_nnzb, cudaStream_t s) {
+  const int mb = (nrows + ts - 1) / ts;
+  DevBuf counts, err;
+  GBS_TRY(counts.alloc(sizeof(int) * ((size_t)mb + 1), s));
+  GBS_TRY(err.alloc(sizeof(int), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(counts.p, 0, sizeof(int) * ((size_t)mb + 1), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  GBS_TRY(pack_dispatch(ts, false, nrows, ncols, mb, rowptr, colind, counts.as<int>(), nullptr, nullptr,
+                        nullptr, err.as<int>(), s));
+  GBS_TRY(exclusive_scan_i32(counts.as<int>(), bsr_rowptr, mb + 1, s));
+  int h[2] = {0, 0};
+  GBS_CUDA_TRY(cudaMemcpyAsync(&h[0], bsr_rowptr + mb, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaMemcpyAsync(&h[1], err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h[1]) return fail(GBS_ERR_INVALID_ARG, "csr2b2sr: column index out of range or columns of a row not ascending");
+  (void)nnz;
+  *h_nnzb = h[0];
+  return GBS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// B2SR x dense B (binary A): one warp per (block-row, group of R tile rows).
+// The 32 lanes describe 32 (tile, column j) entries of the block-row at a
+// time; a ballot keeps the entries that touch any of the warp's rows, and the
+// warp walks them in lane order, gathering the feature row 4*col(t)+j once
+// and adding it to each of its rows whose bit is set (plain FP32 adds, no
+// multiply: A is 0/1).  Entry order: ts = 4 follows spmm4_full_full_new2
+// (spmm.cu:900-943): groups of 8 tiles, column j outer, tile inner, so every
+// output element is the same sequence of additions as the reference and the
+// result is bitwise identical for any FP32 B; other tile sizes use tile then
+// column order (= CSR column order).
+// ---------------------------------------------------------------------------
+struct B2srSpmmArgs {
+  int nrows;  // rows of C written (rows >= nrows are skipped)
+  int mb;
+  const int *rowptr;
+  const int *colind;
+  const void *val;
+  const void *B;
+  int nvec;
+  long long ldb, ldc;
+  float *C;
+};
+
+template <int TS>
+__device__ __forceinline__ uint32_t tile_row(const void *val, size_t t, int r) {
+  using VT = typename TileT<TS>::T;
+  return (uint32_t)__ldg(reinterpret_cast<const VT *>(val) + t * TS + r);
+}
+
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ>
+__global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
+  constexpr int NSUB = 32 / LPR;
+  constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;  // tile rows per warp
+  constexpr int NG = (TS + R - 1) / R;                  // row groups per block-row
+  constexpr int TPG = 32 / TS;                          // tiles per 32 entries
+  constexpr bool REF_ORDER = (TS == 4);
+  constexpr int U = 4;
+  using F_ = Feat<DT, VEC>;
+  using raw = typename F_::raw;
+
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long br = gw / NG;
+  if (br >= a.mb) return;
+  const int row0 = (int)(gw % NG) * R;
+  const int my0 = sub * RPS;  // my first row inside the warp's group
+  const unsigned my_mask = ((1u << RPS) - 1u) << my0;
+
+  float acc[RPS][CH][VEC];
+#pragma unroll
+  for (int k = 0; k < RPS; ++k)
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[k][c][q] = 0.f;
+
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int j = REF_ORDER ? lane / TPG : lane % TS;
+  const int l = REF_ORDER ? lane % TPG : lane / TS;
+  for (int g0 = tb; g0 < te; g0 += TPG) {
+    const int t = g0 + l;
+    unsigned rmask = 0;
+    int brow = 0;
+    if (t < te) {
+      brow = __ldg(a.colind + t) * TS + j;
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        if (row0 + i < TS) rmask |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+    }
+    unsigned act = __ballot_sync(0xffffffffu, rmask != 0);
+    while (act) {
+      raw bv[U][CH];
+      unsigned mu[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = act ? __ffs(act) - 1 : 0;
+        const bool live = act != 0;
+        act &= act - 1;
+        const int col = __shfl_sync(0xffffffffu, brow, e);
+        const unsigned m = __shfl_sync(0xffffffffu, rmask, e);
+        mu[u] = live ? m : 0u;
+        const bool need = (mu[u] & my_mask) != 0;
+        const size_t rb = (size_t)col * (size_t)a.ldb;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          const int chunk = c * LPR + sl;
+          if (need && chunk < a.nvec) bv[u][c] = F_::load(a.B, rb + (size_t)chunk * VEC);
+          else bv[u][c] = F_::zero();
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          float x[VEC];
+          F_::widen(x, bv[u][c]);
+#pragma unroll
+          for (int k = 0; k < RPS; ++k)
+            if ((mu[u] >> (my0 + k)) & 1u)
+#pragma unroll
+              for (int q = 0; q < VEC; ++q) acc[k][c][q] = acc[k][c][q] + x[q];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RPS; ++k) {
+    const int tr = row0 + my0 + k;
+    if (my0 + k >= R || tr >= TS) continue;
+    const long long orow = br * TS + tr;
+    if (orow >= a.nrows) continue;
+    float *dst = a.C + (size_t)orow * a.ldc;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + sl;
+      if (chunk >= a.nvec) continue;
+      if (STORE_NZ) {
+#pragma unroll
+        for (int q = 0; q < VEC; ++q)
+          if (acc[k][c][q] != 0.f) dst[(size_t)chunk * VEC + q] = acc[k][c][q];
+      } else {
+        store_vec<VEC, true>(dst + (size_t)chunk * VEC, acc[k][c]);
+      }
+    }
+  }
+}
+
+namespace {
+
+struct B2srVariant {
+  const void *fn;
+  int vec, lpr, ch, rows_per_warp, groups;
+};
+
+template <int TS, int DT, int VEC, int LPR, int CH, bool NZ>
+B2srVariant mk_b2sr() {
+  constexpr int NSUB = 32 / LPR;
+  constexpr int RPS0 = (32 / (CH * VEC)) > 0 ? (32 / (CH * VEC)) : 1;
+  constexpr int RPS1 = RPS0 > 4 ? 4 : RPS0;
+  constexpr int RPS = (NSUB * RPS1 > TS) ? ((TS / NSUB) > 0 ? TS / NSUB : 1) : RPS1;
+  constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
+  return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
+                     (TS + R - 1) / R};
+}
+
+template <int TS, int DT, int VEC, bool NZ>
+bool pick_b2sr(int nvec, B2srVariant *v) {
+  if (nvec <= 1) { *v = mk_b2sr<TS, DT, VEC, 1, 1, NZ>(); return true; }
+  if (nvec <= 2) { *v = mk_b2sr<TS, DT, VEC, 2, 1, NZ>(); return true; }
+  if (nvec <= 4) { *v = mk_b2sr<TS, DT, VEC, 4, 1, NZ>(); return true; }
+  if (nvec <= 8) { *v = mk_b2sr<TS, DT, VEC, 8, 1, NZ>(); return true; }
+  if (nvec <= 16) { *v = mk_b2sr<TS, DT, VEC, 16, 1, NZ>(); return true; }
+  if (nvec <= 32) { *v = mk_b2sr<TS, DT, VEC, 32, 1, NZ>(); return true; }
+  if (nvec <= 64) { *v = mk_b2sr<TS, DT, VEC, 32, 2, NZ>(); return true; }
+  if (nvec <= 128) { *v = mk_b2sr<TS, DT, VEC, 32, 4, NZ>(); return true; }
+  if (nvec <= 256) { *v = mk_b2sr<TS, DT, VEC, 32, 8, NZ>(); return true; }
+  return false;
+}
+
+template <int TS, bool NZ>
+bool pick_ts(int dt, int F, bool vec16, B2srVariant *v) {
+  if (dt == DT_F32) {
+    if (vec16 && F % 4 == 0) return pick_b2sr<TS, DT_F32, 4, NZ>(F / 4, v);
+    return pick_b2sr<TS, DT_F32, 1, NZ>(F, v);
+  }
+  if (!vec16 || F % 8 != 0) return false;
+  if (dt == DT_BF16) return pick_b2sr<TS, DT_BF16, 8, NZ>(F / 8, v);
+  return pick_b2sr<TS, DT_F16, 8, NZ>(F / 8, v);
+}
+
+bool is_aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *rowptr, const int *colind,
+                         const void *val, const void *B, int dt, int F, float *C, cudaStream_t s) {
+  const bool vec16 = is_aligned16(B) && is_aligned16(C) && F % (dt == DT_F32 ? 4 : 8) == 0;
+  B2srVariant v{};
+  bool ok = false;
+  switch (ts) {
+    case 4: ok = store_nz ? pick_ts<4, true>(dt, F, vec16, &v) : pick_ts<4, false>(dt, F, vec16, &v); break;
+    case 8: ok = store_nz ? pick_ts<8, true>(dt, F, vec16, &v) : pick_ts<8, false>(dt, F, vec16, &v); break;
+    case 16: ok = store_nz ? pick_ts<16, true>(dt, F, vec16, &v) : pick_ts<16, false>(dt, F, vec16, &v); break;
+    case 32: ok = store_nz ? pick_ts<32, true>(dt, F, vec16, &v) : pick_ts<32, false>(dt, F, vec16, &v); break;
+    default: return fail(GBS_ERR_UNSUPPORTED, "b2sr spmm: tile size must be 4, 8, 16 or 32");
+  }
+  if (!ok)
+    return fail(GBS_ERR_UNSUPPORTED,
+                "b2sr spmm: F too large (FP32 <= 1024 with 16-byte alignment, else <= 256; 16-bit "
+                "features need F % 8 == 0, F <= 2048)");
+  if (mb == 0) return GBS_OK;
+  B2srSpmmArgs a;
+  a.nrows = nrows;
+  a.mb = mb;
+  a.rowptr = rowptr;
+  a.colind = colind;
+  a.val = val;
+  a.B = B;
+  a.nvec = F / v.vec;
+  a.ldb = F;
+  a.ldc = F;
+  a.C = C;
+  const long long warps = (long long)mb * v.groups;
+  const int blocks = (int)((warps * 32 + 255) / 256);
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s));
+  return GBS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// B2SR x packed-bit features -> int32 counts (BMV for F = 32, BMM above).
+// X row j = W = ceil(F/32) uint32 words, column 32w+b at bit 31-b of word w
+// (ToBit32RowDenseSign layout, spmm.cu:75-91).  C01[i][k] = sum_j A_ij
+// bit_jk; signed form 2*C01 - deg(i) is the +-1 product.  Lane l owns columns
+// l, l+32, ...; one warp per (block-row, group of R tile rows), R*W <= 32
+// counters per lane.
+// ---------------------------------------------------------------------------
+struct B2srBmmArgs {
+  int nrows, mb, F, W;
+  const int *rowptr;
+  const int *colind;
+  const void *val;
+  const uint32_t *X;
+  int32_t *C;
+  int signed_form;
+};
+
+template <int TS, int WMAX>
+__global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
+  constexpr int R0 = 32 / WMAX > 0 ? 32 / WMAX : 1;
+  constexpr int R = R0 < TS ? R0 : TS;
+  constexpr int NG = (TS + R - 1) / R;
+  constexpr int TPG = 32 / TS;
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long br = gw / NG;
+  if (br >= a.mb) return;
+  const int row0 = (int)(gw % NG) * R;
+  int cnt[R][WMAX];
+  int deg[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    deg[i] = 0;
+#pragma unroll
+    for (int k = 0; k < WMAX; ++k) cnt[i][k] = 0;
+  }
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int j = lane % TS, l = lane / TS;
+  const int shift = 31 - lane;
+  for (int g0 = tb; g0 < te; g0 += TPG) {
+    const int t = g0 + l;
+    unsigned rmask = 0;
+    int brow = 0;
+    if (t < te) {
+      brow = __ldg(a.colind + t) * TS + j;
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        if (row0 + i < TS) rmask |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+    }
+    unsigned act = __ballot_sync(0xffffffffu, rmask != 0);
+    while (act) {
+      const int e = __ffs(act) - 1;
+      act &= act - 1;
+      const int col = __shfl_sync(0xffffffffu, brow, e);
+      const unsigned m = __shfl_sync(0xffffffffu, rmask, e);
+      const uint32_t *xr = a.X + (size_t)col * a.W;
+      uint32_t w[WMAX];
+#pragma unroll
+      for (int k = 0; k < WMAX; ++k) w[k] = k < a.W ? __ldg(xr + k) : 0u;
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        if ((m >> i) & 1u) {
+          ++deg[i];
+#pragma unroll
+          for (int k = 0; k < WMAX; ++k) cnt[i][k] += (int)((w[k] >> shift) & 1u);
+        }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int tr = row0 + i;
+    if (tr >= TS) continue;
+    const long long orow = br * TS + tr;
+    if (orow >= a.nrows) continue;
+    int32_t *dst = a.C + (size_t)orow * a.F;
+#pragma unroll
+    for (int k = 0; k < WMAX; ++k) {
+      const int c = k * 32 + lane;
+      if (c < a.F) dst[c] = a.signed_form ? 2 * cnt[i][k] - deg[i] : cnt[i][k];
+    }
+  }
+}
+
+template <int TS>
+gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
+  const void *fn = nullptr;
+  int wmax = 0;
+  if (a.W <= 1) { fn = (const void *)&k_b2sr_bmm<TS, 1>; wmax = 1; }
+  else if (a.W <= 2) { fn = (const void *)&k_b2sr_bmm<TS, 2>; wmax = 2; }
+  else if (a.W <= 4) { fn = (const void *)&k_b2sr_bmm<TS, 4>; wmax = 4; }
+  else if (a.W <= 8) { fn = (const void *)&k_b2sr_bmm<TS, 8>; wmax = 8; }
+  else if (a.W <= 16) { fn = (const void *)&k_b2sr_bmm<TS, 16>; wmax = 16; }
+  else if (a.W <= 32) { fn = (const void *)&k_b2sr_bmm<TS, 32>; wmax = 32; }
+  else return fail(GBS_ERR_UNSUPPORTED, "b2sr bmm: F must be <= 1024");
+  const int R0 = 32 / wmax > 0 ? 32 / wmax : 1;
+  const int R = R0 < TS ? R0 : TS;
+  const int NG = (TS + R - 1) / R;
+  const long long warps = (long long)a.mb * NG;
+  const int blocks = (int)((warps * 32 + 255) / 256);
+  if (blocks == 0) return GBS_OK;
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s));
+  return GBS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Aligned B2SR-8 / B2SR-16 (packUchar2AlignedUnsigned, :608-648;
+// packUshort2AlignedUnsigned, :859-888): tiles of a block-row padded to a
+// multiple of g = 4 (ts 8) / 2 (ts 16) with colind 0; word j of a group of g
+// tiles holds row j of each, the first tile in the most significant byte
+// (ts 8) / half (ts 16).
+// ---------------------------------------------------------------------------
+__global__ void k_aligned_counts(int mb, int g, const int *__restrict__ brp, int *__restrict__ counts) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < mb) {
+    const int nt = brp[i + 1] - brp[i];
+    counts[i] = (nt + g - 1) / g * g;
+  } else if (i == mb) {
+    counts[i] = 0;
+  }
+}
+
+template <int TS>
+__global__ void __launch_bounds__(256)
+    k_aligned_fill(int mb, const int *__restrict__ brp, const int *__restrict__ bcol, const void *__restrict__ bval,
+                   const int *__restrict__ nrp, int *__restrict__ ncol, uint32_t *__restrict__ nval) {
+  constexpr int g = TS == 8 ? 4 : 2;
+  constexpr int sh = 32 / g;
+  const int lane = threadIdx.x & 31;
+  const long long br = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (br >= mb) return;
+  const int start = brp[br], nt = brp[br + 1] - start;
+  const int pstart = nrp[br], padded = nrp[br + 1] - pstart;
+  for (int i = lane; i < padded; i += 32) ncol[pstart + i] = i < nt ? bcol[start + i] : 0;
+  const long long wbase = (long long)pstart / g * TS;
+  const int nwords = padded / g * TS;
+  for (int w = lane; w < nwords; w += 32) {
+    const int gi = w / TS, j = w % TS;
+    uint32_t word = 0;
+#pragma unroll
+    for (int q = 0; q < g; ++q) {
+      const int ti = gi * g + q;
+      const uint32_t a = ti < nt ? tile_row<TS>(bval, (size_t)start + ti, j) : 0u;
+      word |= a << ((g - 1 - q) * sh);
+    }
+    nval[wbase + w] = word;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dense sign packers: bit = (x >= 0), first column in bit 31.
+//   rows : ToBit32RowDenseSign (spmm.cu:75-91), out[r*W + w]
+//   colud: ToBit32ColUd (spmm.cu:93-111), out[w*Hp + r], Hp = 32*ceil(H/32)
+// Elements outside the matrix read as -1 (bit 0).
+// ---------------------------------------------------------------------------
+template <bool COLUD>
+__global__ void __launch_bounds__(256)
+    k_pack_sign(const float *__restrict__ X, int H, int Wd, int Hp, uint32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int rows = COLUD ? Hp : H;
+  if (row >= rows) return;
+  const int W = (Wd + 31) / 32;
+  for (int w = 0; w < W; ++w) {
+    const int c = w * 32 + lane;
+    const float x = (row < H && c < Wd) ? __ldg(X + (size_t)row * Wd + c) : -1.0f;
+    const uint32_t word = __brev(__ballot_sync(0xffffffffu, x >= 0.0f));
+    if (lane == 0) {
+      if (COLUD) out[(size_t)w * Hp + row] = word;
+      else out[(size_t)row * W + w] = word;
+    }
+  }
+}
+
+}  // namespace gbs
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace gbs;
+
+static bool valid_tile(int t) { return t == 4 || t == 8 || t == 16 || t == 32; }
+
+extern "C" gbs_status gbs_csr2b2sr_nnzb(int nrows, int ncols, int nnz, const int *rowptr,
+                                        const int *colind, int tile, int *bsr_rowptr, int *h_nnzb,
+                                        gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(valid_tile(tile), "csr2b2sr: tile must be 4, 8, 16 or 32");
+  GBS_REQUIRE(nrows >= 0 && ncols >= 0 && nnz >= 0, "csr2b2sr: negative size");
+  GBS_REQUIRE(h_nnzb != nullptr, "csr2b2sr: null nnzb output");
+  GBS_REQUIRE(nrows == 0 || (rowptr != nullptr && bsr_rowptr != nullptr), "csr2b2sr: null pointer");
+  GBS_REQUIRE(nnz == 0 || colind != nullptr, "csr2b2sr: null colind");
+  if (nrows == 0) {
+    *h_nnzb = 0;
+    if (bsr_rowptr) GBS_CUDA_TRY(cudaMemsetAsync(bsr_rowptr, 0, sizeof(int), (cudaStream_t)stream));
+    return GBS_OK;
+  }
+  return b2sr_nnzb(nrows, ncols, nnz, rowptr, colind, tile, bsr_rowptr, h_nnzb, (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_csr2b2sr(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                                   int tile, const int *bsr_rowptr, int *bsr_colind, void *bsr_val,
+                                   gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(valid_tile(tile), "csr2b2sr: tile must be 4, 8, 16 or 32");
+  GBS_REQUIRE(nrows >= 0 && ncols >= 0 && nnz >= 0, "csr2b2sr: negative size");
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(rowptr && bsr_rowptr, "csr2b2sr: null pointer");
+  GBS_REQUIRE(nnz == 0 || (colind && bsr_colind && bsr_val), "csr2b2sr: null pointer");
+  const int mb = (nrows + tile - 1) / tile;
+  return pack_dispatch(tile, true, nrows, ncols, mb, rowptr, colind, nullptr, bsr_rowptr, bsr_colind,
+                       bsr_val, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_csr2bsr_batch(const int *h_rowptr, const int *h_colind, int nrows, int ncols,
+                                        int nnz, int *bsr_rowptr, int *bsr_colind, void *bsr_val,
+                                        int blocksize, int nblockrows, int nblocks) {
+  clear_error();
+  GBS_REQUIRE(valid_tile(blocksize), "csr2bsr_batch: blocksize must be 4, 8, 16 or 32");
+  GBS_REQUIRE(nrows >= 0 && ncols >= 0 && nnz >= 0 && nblocks >= 0, "csr2bsr_batch: negative size");
+  GBS_REQUIRE(nblockrows == (nrows + blocksize - 1) / blocksize,
+              "csr2bsr_batch: nblockrows must be ceil(nrows / blocksize)");
+  GBS_REQUIRE(nrows == 0 || (h_rowptr && bsr_rowptr), "csr2bsr_batch: null pointer");
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(h_rowptr[0] == 0 && h_rowptr[nrows] == nnz, "csr2bsr_batch: rowptr[0] != 0 or rowptr[nrows] != nnz");
+  cudaStream_t s = 0;
+  DevBuf drp, dci;
+  GBS_TRY(drp.alloc(sizeof(int) * ((size_t)nrows + 1), s));
+  GBS_TRY(dci.alloc(sizeof(int) * (size_t)nnz, s));
+  GBS_CUDA_TRY(cudaMemcpyAsync(drp.p, h_rowptr, sizeof(int) * ((size_t)nrows + 1), cudaMemcpyHostToDevice, s));
+  if (nnz > 0)
+    GBS_CUDA_TRY(cudaMemcpyAsync(dci.p, h_colind, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  int got = 0;
+  GBS_TRY(b2sr_nnzb(nrows, ncols, nnz, drp.as<int>(), dci.as<int>(), blocksize, bsr_rowptr, &got, s));
+  if (got != nblocks)
+    return fail(GBS_ERR_INVALID_ARG, "csr2bsr_batch: nblocks = " + std::to_string(nblocks) +
+                                         " but the matrix has " + std::to_string(got) + " tiles");
+  if (nblocks > 0) {
+    GBS_REQUIRE(bsr_colind && bsr_val, "csr2bsr_batch: null output");
+    GBS_TRY(pack_dispatch(blocksize, true, nrows, ncols, nblockrows, drp.as<int>(), dci.as<int>(), nullptr,
+                          bsr_rowptr, bsr_colind, bsr_val, nullptr, s));
+  }
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_b2sr_spmm(int tile, int nrows, int nblockrows, const int *rowptr, const int *colind,
+                                    const void *val, const void *B, gbs_dtype btype, int F, float *C,
+                                    gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(valid_tile(tile), "b2sr spmm: tile must be 4, 8, 16 or 32");
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "b2sr spmm: bad dtype");
+  GBS_REQUIRE(nrows >= 0 && F >= 1, "b2sr spmm: bad sizes");
+  GBS_REQUIRE(nblockrows == (nrows + tile - 1) / tile, "b2sr spmm: nblockrows must be ceil(nrows / tile)");
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(rowptr && C && B, "b2sr spmm: null pointer");
+  const int dt = btype == GBS_F32 ? DT_F32 : (btype == GBS_BF16 ? DT_BF16 : DT_F16);
+  return b2sr_spmm_run(tile, false, nrows, nblockrows, rowptr, colind, val, B, dt, F, C,
+                       (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_spmm4_full_full(const uint8_t *A, const float *B, float *C, const int *rowptr,
+                                          const int *colind, int nblockrows, int B_cols,
+                                          gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(nblockrows >= 0 && B_cols >= 1, "spmm4_full_full: bad sizes");
+  if (nblockrows == 0) return GBS_OK;
+  GBS_REQUIRE(rowptr && B && C, "spmm4_full_full: null pointer");
+  return b2sr_spmm_run(4, true, nblockrows * 4, nblockrows, rowptr, colind, A, B, DT_F32, B_cols, C,
+                       (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_b2sr_bmm(int tile, int nrows, int nblockrows, const int *rowptr, const int *colind,
+                                   const void *val, const uint32_t *X, int F, int signed_form, int32_t *C,
+                                   gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(valid_tile(tile), "b2sr bmm: tile must be 4, 8, 16 or 32");
+  GBS_REQUIRE(nrows >= 0 && F >= 1 && F <= 1024, "b2sr bmm: need 1 <= F <= 1024");
+  GBS_REQUIRE(nblockrows == (nrows + tile - 1) / tile, "b2sr bmm: nblockrows must be ceil(nrows / tile)");
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(rowptr && C && X, "b2sr bmm: null pointer");
+  B2srBmmArgs a;
+  a.nrows = nrows;
+  a.mb = nblockrows;
+  a.F = F;
+  a.W = (F + 31) / 32;
+  a.rowptr = rowptr;
+  a.colind = colind;
+  a.val = val;
+  a.X = X;
+  a.C = C;
+  a.signed_form = signed_form ? 1 : 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (tile) {
+    case 4: return launch_bmm<4>(a, s);
+    case 8: return launch_bmm<8>(a, s);
+    case 16: return launch_bmm<16>(a, s);
+    default: return launch_bmm<32>(a, s);
+  }
+}
+
+extern "C" gbs_status gbs_b2sr_aligned_nnzb(int tile, int nblockrows, const int *bsr_rowptr, int *new_rowptr,
+                                            int *h_ntiles, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(tile == 8 || tile == 16, "b2sr aligned: tile must be 8 or 16");
+  GBS_REQUIRE(nblockrows >= 0 && h_ntiles, "b2sr aligned: bad arguments");
+  GBS_REQUIRE(bsr_rowptr && new_rowptr, "b2sr aligned: null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  DevBuf counts;
+  GBS_TRY(counts.alloc(sizeof(int) * ((size_t)nblockrows + 1), s));
+  const int g = tile == 8 ? 4 : 2;
+  k_aligned_counts<<<(nblockrows + 1 + 255) / 256, 256, 0, s>>>(nblockrows, g, bsr_rowptr, counts.as<int>());
+  GBS_TRY(check_launch("k_aligned_counts"));
+  GBS_TRY(exclusive_scan_i32(counts.as<int>(), new_rowptr, nblockrows + 1, s));
+  int h = 0;
+  GBS_CUDA_TRY(cudaMemcpyAsync(&h, new_rowptr + nblockrows, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  *h_ntiles = h;
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_b2sr_pack_aligned(int tile, int nblockrows, const int *bsr_rowptr,
+                                            const int *bsr_colind, const void *bsr_val, const int *new_rowptr,
+                                            int *new_colind, uint32_t *new_val, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(tile == 8 || tile == 16, "b2sr aligned: tile must be 8 or 16");
+  GBS_REQUIRE(nblockrows >= 0, "b2sr aligned: bad sizes");
+  if (nblockrows == 0) return GBS_OK;
+  GBS_REQUIRE(bsr_rowptr && new_rowptr && new_colind && new_val, "b2sr aligned: null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = (int)(((long long)nblockrows * 32 + 255) / 256);
+  if (tile == 8)
+    k_aligned_fill<8><<<blocks, 256, 0, s>>>(nblockrows, bsr_rowptr, bsr_colind, bsr_val, new_rowptr, new_colind, new_val);
+  else
+    k_aligned_fill<16><<<blocks, 256, 0, s>>>(nblockrows, bsr_rowptr, bsr_colind, bsr_val, new_rowptr, new_colind, new_val);
+  return check_launch("k_aligned_fill");
+}
+
+extern "C" gbs_status gbs_pack_sign_rows(const float *X, int n, int F, uint32_t *out, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(n >= 0 && F >= 1, "pack_sign_rows: bad sizes");
+  if (n == 0) return GBS_OK;
+  GBS_REQUIRE(X && out, "pack_sign_rows: null pointer");
+  const int blocks = (int)(((long long)n * 32 + 255) / 256);
+  k_pack_sign<false><<<blocks, 256, 0, (cudaStream_t)stream>>>(X, n, F, 0, out);
+  return check_launch("k_pack_sign");
+}
+
+extern "C" gbs_status gbs_pack_sign_colud(const float *A, int H, int Wd, uint32_t *out, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(H >= 0 && Wd >= 1, "pack_sign_colud: bad sizes");
+  if (H == 0) return GBS_OK;
+  GBS_REQUIRE(A && out, "pack_sign_colud: null pointer");
+  const int Hp = (H + 31) / 32 * 32;
+  const int blocks = (int)(((long long)Hp * 32 + 255) / 256);
+  k_pack_sign<true><<<blocks, 256, 0, (cudaStream_t)stream>>>(A, H, Wd, Hp, out);
+  return check_launch("k_pack_sign");
+}

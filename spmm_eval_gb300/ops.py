@@ -110,3 +110,126 @@ def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
               _ptr(A.vals), _ptr(B), _DT[B.dtype], F, int(col_block), _ptr(out), _ptr(buf),
               buf.numel(), _stream(B.device))
     return out
+
+
+# ---------------------------------------------------------------------------
+# B2SR
+# ---------------------------------------------------------------------------
+_TILE_DT = {4: torch.uint8, 8: torch.uint8, 16: torch.int16, 32: torch.int32}
+
+
+@dataclass
+class B2SR:
+    """B2SR matrix on the device: tile rows as uint8 (tile 4, 8), 16-bit
+    (tile 16) or 32-bit (tile 32) words held in torch tensors of that width."""
+
+    rowptr: torch.Tensor
+    colind: torch.Tensor
+    val: torch.Tensor
+    tile: int
+    nrows: int
+    ncols: int
+
+    @property
+    def nblockrows(self) -> int:
+        return (self.nrows + self.tile - 1) // self.tile
+
+    @property
+    def nnzb(self) -> int:
+        return int(self.colind.numel())
+
+
+def csr2b2sr(A: CSR, tile: int) -> B2SR:
+    """Pack a CSR matrix (values ignored) into B2SR with the given tile."""
+    A.validate_layout()
+    dev = A.rowptr.device
+    mb = (A.nrows + tile - 1) // tile
+    rowptr = torch.empty(mb + 1, dtype=torch.int32, device=dev)
+    nnzb = C.c_int(0)
+    s = _stream(dev)
+    _lib.call("gbs_csr2b2sr_nnzb", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind), tile,
+              _ptr(rowptr), C.byref(nnzb), s)
+    nb = int(nnzb.value)
+    colind = torch.empty(max(nb, 1), dtype=torch.int32, device=dev)[:nb]
+    val = torch.empty(max(nb * tile, 1), dtype=_TILE_DT[tile], device=dev)[:nb * tile]
+    _lib.call("gbs_csr2b2sr", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind), tile,
+              _ptr(rowptr), _ptr(colind), _ptr(val), s)
+    return B2SR(rowptr, colind, val, tile, A.nrows, A.ncols)
+
+
+def b2sr_spmm(Ab: B2SR, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """C = A01 @ B (FP32 out).  Tile 4 reproduces spmm4_full_full_new2's
+    addition order exactly."""
+    _check_cuda("B", B, tuple(_DT))
+    F = int(B.shape[1])
+    if out is None:
+        out = torch.empty((Ab.nrows, F), dtype=torch.float32, device=B.device)
+    _lib.call("gbs_b2sr_spmm", Ab.tile, Ab.nrows, Ab.nblockrows, _ptr(Ab.rowptr), _ptr(Ab.colind),
+              _ptr(Ab.val), _ptr(B), _DT[B.dtype], F, _ptr(out), _stream(B.device))
+    return out
+
+
+def spmm4_full_full(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, rowptr: torch.Tensor,
+                    colind: torch.Tensor, nblockrows: int, B_cols: int) -> None:
+    """Mirror of the reference launch spmm4_full_full_new2<<<...>>>(A, B, C,
+    rowptr, colind, nblockrows, B_cols): C must be zero-filled; only nonzero
+    results are stored."""
+    _lib.call("gbs_spmm4_full_full", _ptr(A), _ptr(B), _ptr(C_), _ptr(rowptr), _ptr(colind),
+              int(nblockrows), int(B_cols), _stream(B.device))
+
+
+def csr2bsr_batch(h_rowptr, h_colind, nrows: int, ncols: int, nnz: int, bsrRowPtr: torch.Tensor,
+                  bsrColInd: torch.Tensor, bsrVal: torch.Tensor, blocksize: int, nblockrows: int,
+                  nblocks: int) -> None:
+    """Mirror of csr2bsr_batch_{4,8,16,32}: host CSR (numpy int32 arrays),
+    caller-allocated device outputs."""
+    import numpy as np
+    h_rowptr = np.ascontiguousarray(h_rowptr, dtype=np.int32)
+    h_colind = np.ascontiguousarray(h_colind, dtype=np.int32)
+    _lib.call("gbs_csr2bsr_batch", h_rowptr.ctypes.data, h_colind.ctypes.data if h_colind.size else None,
+              nrows, ncols, nnz, _ptr(bsrRowPtr), _ptr(bsrColInd), _ptr(bsrVal), blocksize,
+              nblockrows, nblocks)
+
+
+def pack_sign_rows(X: torch.Tensor) -> torch.Tensor:
+    """bit = (x >= 0) packed along columns, ceil(F/32) int32-held words/row."""
+    _check_cuda("X", X, torch.float32)
+    n, F = X.shape
+    out = torch.empty((n, (F + 31) // 32), dtype=torch.int32, device=X.device)
+    _lib.call("gbs_pack_sign_rows", _ptr(X), n, F, _ptr(out), _stream(X.device))
+    return out
+
+
+def pack_sign_colud(X: torch.Tensor) -> torch.Tensor:
+    """ToBit32ColUd layout: [ceil(W/32)][32*ceil(H/32)] words."""
+    _check_cuda("X", X, torch.float32)
+    H, W = X.shape
+    out = torch.empty(((W + 31) // 32, (H + 31) // 32 * 32), dtype=torch.int32, device=X.device)
+    _lib.call("gbs_pack_sign_colud", _ptr(X), H, W, _ptr(out), _stream(X.device))
+    return out
+
+
+def b2sr_bmm(Ab: B2SR, Xbits: torch.Tensor, F: int, signed_form: bool = False) -> torch.Tensor:
+    """int32 C[i][k] = sum_j A_ij bit_jk (or 2*C - deg(i) when signed)."""
+    _check_cuda("Xbits", Xbits, torch.int32)
+    out = torch.empty((Ab.nrows, F), dtype=torch.int32, device=Xbits.device)
+    _lib.call("gbs_b2sr_bmm", Ab.tile, Ab.nrows, Ab.nblockrows, _ptr(Ab.rowptr), _ptr(Ab.colind),
+              _ptr(Ab.val), _ptr(Xbits), F, int(signed_form), _ptr(out), _stream(Xbits.device))
+    return out
+
+
+def b2sr_aligned(Ab: B2SR):
+    """Aligned B2SR-8/16: (rowptr, colind, uint32-held words)."""
+    dev = Ab.rowptr.device
+    mb = Ab.nblockrows
+    nrp = torch.empty(mb + 1, dtype=torch.int32, device=dev)
+    nt = C.c_int(0)
+    s = _stream(dev)
+    _lib.call("gbs_b2sr_aligned_nnzb", Ab.tile, mb, _ptr(Ab.rowptr), _ptr(nrp), C.byref(nt), s)
+    g = 4 if Ab.tile == 8 else 2
+    ntiles = int(nt.value)
+    ncol = torch.empty(max(ntiles, 1), dtype=torch.int32, device=dev)[:ntiles]
+    nval = torch.empty(max(ntiles * Ab.tile // g, 1), dtype=torch.int32, device=dev)[:ntiles * Ab.tile // g]
+    _lib.call("gbs_b2sr_pack_aligned", Ab.tile, mb, _ptr(Ab.rowptr), _ptr(Ab.colind), _ptr(Ab.val),
+              _ptr(nrp), _ptr(ncol), _ptr(nval), s)
+    return nrp, ncol, nval

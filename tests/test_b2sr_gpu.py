@@ -1,0 +1,266 @@
+"""GPU parity of the B2SR path: packing (bit-exact vs the oracle, vs the
+hand-derived known answers, and vs cuSPARSE csr2bsr -- the library call the
+reference's packer is built on), B2SR x dense SpMM (tile 4 bitwise equal to
+the reference's summation order; all tiles bit-exact against the CSR
+product on 0/1 and +-1 features, and equal to cusparseSpMM on +-1 features
+as the reference driver checks, test_spmm_full.cu:421-431), B2SR x bits BMM
+(bit-exact int32), the aligned formats and the dense sign packers."""
+import ctypes as C
+import json
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from spmm_eval_gb300 import _lib
+from spmm_eval_gb300 import graphs as G
+from spmm_eval_gb300 import ops
+
+pytestmark = pytest.mark.gpu
+HERE = Path(__file__).resolve().parent
+TILES = [4, 8, 16, 32]
+NPDT = {4: np.uint8, 8: np.uint8, 16: np.uint16, 32: np.uint32}
+
+
+@pytest.fixture(scope="session")
+def cusparse_ref(cuda):
+    so = HERE / "native" / "libcusparse_ref.so"
+    src = HERE / "native" / "cusparse_ref.cu"
+    if not so.exists() or so.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-shared",
+                        "-Xcompiler", "-fPIC", "-Wno-deprecated-declarations", "-o", str(so), str(src),
+                        "-lcusparse"], check=True)
+    return C.CDLL(str(so))
+
+
+def graphs():
+    rng = np.random.default_rng(0)
+    out = []
+    d = json.loads((HERE / "golden" / "b2sr_kat.json").read_text())
+    rp = np.zeros(d["nrows"] + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in d["rows"]])
+    ci = np.array([c for r in d["rows"] for c in r], np.int32)
+    out.append(("kat", d["nrows"], d["ncols"], rp, ci))
+    for n, m, dens, dup in [(101, 77, 0.08, False), (257, 300, 0.03, True), (64, 64, 0.5, False)]:
+        rows = []
+        for r in range(n):
+            k = rng.binomial(m, dens) if r % 7 else 0
+            cols = np.sort(rng.choice(m, size=k, replace=False)) if k else np.zeros(0, np.int64)
+            if dup and k:
+                cols = np.sort(np.concatenate([cols, cols[:1]]))
+            rows.append(cols)
+        rp = np.zeros(n + 1, np.int32)
+        rp[1:] = np.cumsum([len(x) for x in rows])
+        out.append((f"rand{n}", n, m, rp, np.concatenate(rows).astype(np.int32)))
+    g = G.flickr_like()
+    out.append(("flickr_like", g.nrows, g.ncols, g.rowptr.numpy(), g.colind.numpy()))
+    return out
+
+
+GRAPHS = graphs()
+
+
+def dev_csr(n, m, rp, ci, dev):
+    return ops.CSR(torch.from_numpy(rp).to(dev), torch.from_numpy(ci).to(dev), None, n, m)
+
+
+def host_val(Ab):
+    v = Ab.val.cpu().numpy()
+    return v.view(NPDT[Ab.tile]) if v.dtype.itemsize == np.dtype(NPDT[Ab.tile]).itemsize else v
+
+
+@pytest.mark.parametrize("ts", TILES)
+@pytest.mark.parametrize("gi", range(len(GRAPHS)))
+def test_pack_bit_exact_vs_oracle(cuda, ts, gi):
+    name, n, m, rp, ci = GRAPHS[gi]
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    assert np.array_equal(Ab.rowptr.cpu().numpy(), brp)
+    assert np.array_equal(Ab.colind.cpu().numpy(), bci)
+    assert np.array_equal(host_val(Ab), bv)
+
+
+@pytest.mark.parametrize("ts", TILES)
+def test_pack_known_answers(cuda, ts):
+    d = json.loads((HERE / "golden" / "b2sr_kat.json").read_text())
+    _, n, m, rp, ci = GRAPHS[0]
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    want = d["packings"][str(ts)]
+    assert Ab.rowptr.cpu().tolist() == want["rowptr"]
+    assert Ab.colind.cpu().tolist() == want["colind"]
+    assert [int(x) for x in host_val(Ab)] == want["val"]
+
+
+@pytest.mark.parametrize("ts", TILES)
+@pytest.mark.parametrize("gi", [1, 2, 4])
+def test_pack_vs_cusparse_csr2bsr(cuda, cusparse_ref, ts, gi):
+    """cusparseXcsr2bsrNnz + cusparseScsr2bsr on the same CSR with values
+    1.0 (as csr2bsr_batch_bsrbmv.cu:296-311 does), then bit = (value > 0) in
+    the ToBit*Col layout, must equal our packing."""
+    name, n, m, rp, ci = GRAPHS[gi]
+    drp = torch.from_numpy(rp).to(cuda)
+    dci = torch.from_numpy(ci).to(cuda)
+    mb = (n + ts - 1) // ts
+    crp = torch.zeros(mb + 1, dtype=torch.int32, device=cuda)
+    nnzb = C.c_int(0)
+    assert cusparse_ref.ref_csr2bsr_nnz(n, m, C.c_void_p(drp.data_ptr()), C.c_void_p(dci.data_ptr()), ts,
+                                        C.c_void_p(crp.data_ptr()), C.byref(nnzb)) == 0
+    nb = nnzb.value
+    ccol = torch.zeros(max(nb, 1), dtype=torch.int32, device=cuda)
+    cval = torch.zeros(max(nb * ts * ts, 1), dtype=torch.float32, device=cuda)
+    ones = torch.ones(max(len(ci), 1), dtype=torch.float32, device=cuda)
+    assert cusparse_ref.ref_csr2bsr_fill(n, m, C.c_void_p(ones.data_ptr()), C.c_void_p(drp.data_ptr()),
+                                         C.c_void_p(dci.data_ptr()), ts, C.c_void_p(cval.data_ptr()),
+                                         C.c_void_p(crp.data_ptr()), C.c_void_p(ccol.data_ptr())) == 0
+    dense = (cval[: nb * ts * ts].reshape(nb, ts, ts) > 0).cpu().numpy().astype(np.uint64)
+    weights = (1 << np.arange(ts - 1, -1, -1, dtype=np.uint64))
+    want_val = (dense * weights[None, None, :]).sum(-1).reshape(-1)
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    assert np.array_equal(Ab.rowptr.cpu().numpy(), crp.cpu().numpy())
+    assert np.array_equal(Ab.colind.cpu().numpy(), ccol[:nb].cpu().numpy())
+    assert np.array_equal(host_val(Ab).astype(np.uint64), want_val)
+
+
+@pytest.mark.parametrize("ts", TILES)
+def test_csr2bsr_batch_dropin(cuda, ts):
+    name, n, m, rp, ci = GRAPHS[2]
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    mb = (n + ts - 1) // ts
+    d_rp = torch.zeros(mb + 1, dtype=torch.int32, device=cuda)
+    d_ci = torch.zeros(len(bci), dtype=torch.int32, device=cuda)
+    d_v = torch.zeros(len(bv), dtype=ops._TILE_DT[ts], device=cuda)
+    ops.csr2bsr_batch(rp, ci, n, m, len(ci), d_rp, d_ci, d_v, ts, mb, len(bci))
+    assert np.array_equal(d_rp.cpu().numpy(), brp)
+    assert np.array_equal(d_ci.cpu().numpy(), bci)
+    assert np.array_equal(d_v.cpu().numpy().view(NPDT[ts]), bv)
+    with pytest.raises(_lib.GbsError):  # wrong nblocks is reported, not written past
+        ops.csr2bsr_batch(rp, ci, n, m, len(ci), d_rp, d_ci, d_v, ts, mb, len(bci) + 1)
+
+
+def test_pack_rejects_bad_csr(cuda):
+    rp = torch.tensor([0, 2, 3], dtype=torch.int32, device=cuda)
+    bad_order = ops.CSR(rp, torch.tensor([5, 3, 1], dtype=torch.int32, device=cuda), None, 2, 10)
+    with pytest.raises(_lib.GbsError, match="ascending"):
+        ops.csr2b2sr(bad_order, 4)
+    bad_range = ops.CSR(rp, torch.tensor([1, 3, 10], dtype=torch.int32, device=cuda), None, 2, 10)
+    with pytest.raises(_lib.GbsError, match="range"):
+        ops.csr2b2sr(bad_range, 8)
+
+
+@pytest.mark.parametrize("gi", range(len(GRAPHS)))
+@pytest.mark.parametrize("F", [32, 64, 128, 256])
+def test_fbf_tile4_bitwise_reference_order(cuda, gi, F):
+    """Arbitrary FP32 features: tile 4 equals the reference's addition order
+    bit for bit (both the full-output entry point and the drop-in that only
+    stores nonzero results into a zero-filled C)."""
+    name, n, m, rp, ci = GRAPHS[gi]
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, 4)
+    rng = np.random.default_rng(F + gi)
+    B = (rng.standard_normal((m, F)) * 10.0 ** rng.integers(-3, 4, (m, 1))).astype(np.float32)
+    want = oracle.b2sr4_spmm_ref(n, brp, bci, bv, B)
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), 4)
+    Bd = torch.from_numpy(B).to(cuda)
+    got = ops.b2sr_spmm(Ab, Bd).cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    mb = (n + 3) // 4
+    Cd = torch.zeros((mb * 4, F), device=cuda)
+    ops.spmm4_full_full(Ab.val, Bd, Cd, Ab.rowptr, Ab.colind, mb, F)
+    assert np.array_equal(Cd[:n].cpu().numpy().view(np.uint32), want.view(np.uint32))
+    assert torch.count_nonzero(Cd[n:]) == 0
+
+
+@pytest.mark.parametrize("ts", TILES)
+@pytest.mark.parametrize("F", [8, 32, 96, 256, 1024])
+def test_b2sr_spmm_exact_on_binary_features(cuda, ts, F):
+    """0/1 and +-1 features: every tile size equals the CSR product exactly
+    (all partial sums are small integers)."""
+    g = G.flickr_like()
+    A = ops.CSR(g.rowptr.to(cuda), g.colind.to(cuda), None, g.nrows, g.ncols)
+    Ab = ops.csr2b2sr(A, ts)
+    rng = np.random.default_rng(ts * F)
+    B01 = torch.from_numpy(rng.integers(0, 2, (g.ncols, F)).astype(np.float32)).to(cuda)
+    assert torch.equal(ops.b2sr_spmm(Ab, B01), ops.csr_spmm(A, B01))
+    Bpm = 2 * B01 - 1
+    assert torch.equal(ops.b2sr_spmm(Ab, Bpm), ops.csr_spmm(A, Bpm))
+
+
+@pytest.mark.parametrize("ts", TILES)
+def test_b2sr_spmm_float_features_vs_oracle(cuda, ts):
+    name, n, m, rp, ci = GRAPHS[4]
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    B = G.normal(ts, 3, (m, 64)).numpy()
+    want = oracle.b2sr_spmm(ts, n, brp, bci, bv, B)
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    got = ops.b2sr_spmm(Ab, torch.from_numpy(B).to(cuda)).cpu().numpy()
+    ref, mag = oracle.csr_spmm_f64(rp, ci, None, B)
+    assert oracle.rel_err(got, ref, mag)[0] <= 1e-5
+    assert oracle.rel_err(want, ref, mag)[0] <= 1e-5
+
+
+@pytest.mark.parametrize("F", [32, 64, 256])
+def test_fbf_equals_cusparse_on_pm1(cuda, cusparse_ref, F):
+    """The reference driver's own check: B2SR-4 FBF == cusparseSpMM (FP32,
+    column-major copies) exactly, for +-1 features and 0/1 A."""
+    g = G.flickr_like()
+    n = g.nrows
+    rng = np.random.default_rng(F)
+    Bh = np.where(rng.random((n, F)) > 0.5, 1.0, -1.0).astype(np.float32)
+    ones = torch.ones(g.nnz, device=cuda)
+    drp, dci = g.rowptr.to(cuda), g.colind.to(cuda)
+    Bcol = torch.from_numpy(np.ascontiguousarray(Bh.T)).to(cuda)
+    Ccol = torch.zeros((F, n), device=cuda)
+    assert cusparse_ref.ref_spmm_colmajor(n, n, g.nnz, C.c_void_p(drp.data_ptr()), C.c_void_p(dci.data_ptr()),
+                                          C.c_void_p(ones.data_ptr()), C.c_void_p(Bcol.data_ptr()), F,
+                                          C.c_void_p(Ccol.data_ptr())) == 0
+    Ab = ops.csr2b2sr(ops.CSR(drp, dci, None, n, n), 4)
+    mb = Ab.nblockrows
+    Cd = torch.zeros((mb * 4, F), device=cuda)
+    ops.spmm4_full_full(Ab.val, torch.from_numpy(Bh).to(cuda), Cd, Ab.rowptr, Ab.colind, mb, F)
+    assert torch.equal(Cd[:n], Ccol.T.contiguous())
+
+
+@pytest.mark.parametrize("ts", TILES)
+@pytest.mark.parametrize("F", [1, 32, 64, 96, 256, 1024])
+def test_bmm_bit_exact(cuda, ts, F):
+    name, n, m, rp, ci = GRAPHS[4] if F <= 256 else GRAPHS[2]
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    X = G.normal(F + ts, 8, (m, F))
+    Xw = ops.pack_sign_rows(X.to(cuda))
+    assert np.array_equal(Xw.cpu().numpy().view(np.uint32), oracle.pack_sign_rows(X.numpy()))
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    for signed in (False, True):
+        got = ops.b2sr_bmm(Ab, Xw, F, signed).cpu().numpy()
+        want = oracle.b2sr_bmm(ts, n, brp, bci, bv, Xw.cpu().numpy().view(np.uint32), F, signed)
+        assert np.array_equal(got, want)
+
+
+def test_bmm_signed_matches_fbf_on_pm1(cuda):
+    """signed BMM == float FBF product with the +-1 features it encodes."""
+    g = G.flickr_like()
+    A = ops.CSR(g.rowptr.to(cuda), g.colind.to(cuda), None, g.nrows, g.ncols)
+    Ab = ops.csr2b2sr(A, 4)
+    X = G.normal(1, 8, (g.ncols, 128)).to(cuda)
+    pm = torch.where(X >= 0, 1.0, -1.0)
+    assert torch.equal(ops.b2sr_bmm(Ab, ops.pack_sign_rows(X), 128, True).float(), ops.b2sr_spmm(Ab, pm))
+
+
+@pytest.mark.parametrize("ts", [8, 16])
+def test_aligned_formats(cuda, ts):
+    for gi in (1, 4):
+        name, n, m, rp, ci = GRAPHS[gi]
+        brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+        nrp, nci, nv = oracle.b2sr_aligned(ts, brp, bci, bv)
+        Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+        grp, gci, gv = ops.b2sr_aligned(Ab)
+        assert np.array_equal(grp.cpu().numpy(), nrp)
+        assert np.array_equal(gci.cpu().numpy(), nci)
+        assert np.array_equal(gv.cpu().numpy().view(np.uint32), nv)
+
+
+def test_pack_sign_colud(cuda):
+    X = G.normal(4, 4, (70, 100))
+    got = ops.pack_sign_colud(X.to(cuda)).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, oracle.pack_sign_colud(X.numpy()))
