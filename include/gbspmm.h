@@ -190,6 +190,33 @@ GBS_API gbs_status gbs_pack_sign_rows(const float *d_X, int n, int F, uint32_t *
 GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t *d_out,
                                gbs_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Dense binary matmul (backend/mm.cu).  A: Kw x M and B: Kw x N uint32
+ * words in the word-major layout of ToBit32ColUd (spmm.cu:93-111), word kw
+ * of row r = K-bits 32kw..32kw+31.  M and N multiples of 4, A and B 16-byte
+ * aligned.
+ * ------------------------------------------------------------------------ */
+/* C (M x N int32, row-major): mode 0 = sum popc(a ^ b), 1 = sum popc(a & b),
+ * 2 = 32*Kw - 2*xor (the +-1 dot product).  algo 0 = default (the faster
+ * on GB300: CUDA-core __popc), 1 = CUDA-core __popc, 2 = tensor-core
+ * mma.sync .b1 AND-popc (XOR from row popcounts). */
+GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
+                      int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
+/* Drop-in for BMM32_Arow_Brow<float> (mm.cu:17-53) and BMM32_MT_M_S
+ * (:59-75): C[r*B_width + c] = 32*A_width - 2*xor as float. */
+GBS_API gbs_status gbs_bmm32_arow_brow(const uint32_t *d_A, const uint32_t *d_B, float *d_C,
+                               int A_height, int A_width, int B_width,
+                               gbs_stream_t stream);
+/* Drop-ins for BMM32_BIN (mm.cu:79-105) and BMM32S_BIN (:108-125): bit =
+ * (n - 2*xor >= 0) with n the number of K bits, 32 output columns per word,
+ * first column in bit 31, stored at C[by*m + r] (BIN) or
+ * C[(r/32)*k*32 + by*32 + r%32] (S_BIN).  m, k multiples of 32.  Allocates
+ * an m x k int32 temporary (stream-ordered). */
+GBS_API gbs_status gbs_bmm32_bin(const uint32_t *d_A, const uint32_t *d_B, uint32_t *d_C,
+                         int m, int n, int k, gbs_stream_t stream);
+GBS_API gbs_status gbs_bmm32s_bin(const uint32_t *d_A, const uint32_t *d_B, uint32_t *d_C,
+                          int m, int n, int k, gbs_stream_t stream);
+
 /* CSR SpMM that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not allocate while they run (a
  * framework that reserves its device memory up front in its own pool, a

@@ -233,3 +233,37 @@ def b2sr_aligned(Ab: B2SR):
     _lib.call("gbs_b2sr_pack_aligned", Ab.tile, mb, _ptr(Ab.rowptr), _ptr(Ab.colind), _ptr(Ab.val),
               _ptr(nrp), _ptr(ncol), _ptr(nval), s)
     return nrp, ncol, nval
+
+
+# ---------------------------------------------------------------------------
+# Dense binary matmul (word-major operands, ToBit32ColUd layout)
+# ---------------------------------------------------------------------------
+BMM_XOR, BMM_AND, BMM_SIGNED = 0, 1, 2
+BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA = 0, 1, 2
+
+
+def bmm_b1(A: torch.Tensor, B: torch.Tensor, mode: int = BMM_XOR, algo: int = BMM_ALGO_DEFAULT,
+           out: torch.Tensor | None = None) -> torch.Tensor:
+    """A: (Kw, M), B: (Kw, N) int32-held words -> int32 (M, N) counts."""
+    _check_cuda("A", A, torch.int32)
+    _check_cuda("B", B, torch.int32)
+    Kw, M = A.shape
+    N = B.shape[1]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.int32, device=A.device)
+    _lib.call("gbs_bmm_b1", _ptr(A), _ptr(B), M, N, Kw, mode, algo, _ptr(out), _stream(A.device))
+    return out
+
+
+def bmm32_arow_brow(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, A_height: int, A_width: int,
+                    B_width: int) -> None:
+    """Mirror of BMM32_Arow_Brow<float>(A, B, C, A_height, A_width, B_width)."""
+    _lib.call("gbs_bmm32_arow_brow", _ptr(A), _ptr(B), _ptr(C_), A_height, A_width, B_width,
+              _stream(A.device))
+
+
+def bmm32_bin(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, m: int, n: int, k: int,
+              s_layout: bool = False) -> None:
+    """Mirror of BMM32_BIN (or BMM32S_BIN with s_layout=True)."""
+    _lib.call("gbs_bmm32s_bin" if s_layout else "gbs_bmm32_bin", _ptr(A), _ptr(B), _ptr(C_), m, n, k,
+              _stream(A.device))
