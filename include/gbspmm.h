@@ -104,6 +104,45 @@ GBS_API gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz,
                             float *d_C, gbs_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Backward of C = A * B (no counterpart in the reference, which has no
+ * differentiation): dB = A^T dC through a cached transpose, and
+ * d(values)[e] = <dC[row(e)], B[col(e)]> (SDDMM on A's pattern).
+ * ------------------------------------------------------------------------ */
+typedef struct gbs_csr_transpose gbs_csr_transpose;
+
+/* Builds A^T (ncols x nrows CSR, rows ascending inside each column, as
+ * csr2csc in backend/readMtx.hpp:319-345) and perm (A^T entry i is A entry
+ * perm[i]).  Allocates the handle's device arrays; synchronises the stream. */
+GBS_API gbs_status gbs_csr_transpose_create(int nrows, int ncols, int nnz,
+                                    const int *d_rowptr, const int *d_colind,
+                                    gbs_stream_t stream, gbs_csr_transpose **out);
+/* Device arrays owned by the handle (any output pointer may be NULL). */
+GBS_API gbs_status gbs_csr_transpose_arrays(const gbs_csr_transpose *T,
+                                    const int **d_t_rowptr, const int **d_t_colind,
+                                    const int **d_perm);
+/* Copies the handle's arrays into caller buffers (any may be NULL). */
+GBS_API gbs_status gbs_csr_transpose_copy(const gbs_csr_transpose *T, int *d_t_rowptr,
+                                  int *d_t_colind, int *d_perm, gbs_stream_t stream);
+/* t_vals[i] = vals[perm[i]]: A's values in A^T order. */
+GBS_API gbs_status gbs_csr_transpose_values(const gbs_csr_transpose *T,
+                                    const float *d_vals, float *d_t_vals,
+                                    gbs_stream_t stream);
+GBS_API gbs_status gbs_csr_transpose_destroy(gbs_csr_transpose *T);
+/* dB (ncols x F, FP32) = A^T dC (dC nrows x F in dtype) with the merge-path
+ * SpMM; t_vals from gbs_csr_transpose_values (NULL: binary A).  Workspace
+ * as gbs_csr_spmm for (ncols, nnz, F, dtype). */
+GBS_API gbs_status gbs_csr_spmm_transposed(const gbs_csr_transpose *T,
+                                   const float *d_t_vals, const void *d_dC,
+                                   gbs_dtype dtype, int F, float *d_dB,
+                                   void *d_workspace, size_t workspace_bytes,
+                                   gbs_stream_t stream);
+/* out[e] = sum_k G[row(e)][k] * H[col(e)][k], FP32 accumulation; G nrows x F
+ * and H ncols x F in dtype. */
+GBS_API gbs_status gbs_sddmm(int nrows, int ncols, int nnz, const int *d_rowptr,
+                     const int *d_colind, const void *d_G, const void *d_H,
+                     gbs_dtype dtype, int F, float *d_out, gbs_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * CSR -> B2SR packing (tile = 4, 8, 16 or 32)
  *
  * B2SR layout (the reference's): block-row i covers CSR rows [i*tile,

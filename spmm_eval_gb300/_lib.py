@@ -41,6 +41,13 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_csr_spmm_cb": (st, [i32, i32, i32, p, p, p, p, i32, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_f32": (st, [i32, i32, i32, p, p, p, p, i32, p, p]),
     "gbs_csr_spmm_noalloc": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
+    "gbs_csr_transpose_create": (st, [i32, i32, i32, p, p, p, C.POINTER(p)]),
+    "gbs_csr_transpose_arrays": (st, [p, C.POINTER(p), C.POINTER(p), C.POINTER(p)]),
+    "gbs_csr_transpose_copy": (st, [p, p, p, p, p]),
+    "gbs_csr_transpose_values": (st, [p, p, p, p]),
+    "gbs_csr_transpose_destroy": (st, [p]),
+    "gbs_csr_spmm_transposed": (st, [p, p, p, i32, i32, p, p, sz, p]),
+    "gbs_sddmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr2b2sr_nnzb": (st, [i32, i32, i32, p, p, i32, p, pi32, p]),
     "gbs_csr2b2sr": (st, [i32, i32, i32, p, p, i32, p, p, p, p]),
     "gbs_csr2bsr_batch": (st, [p, p, i32, i32, i32, p, p, p, i32, i32, i32]),

@@ -23,6 +23,7 @@
 #include "common.cuh"
 #include "csr_spmm.cuh"
 #include "feat.cuh"
+#include "merge.cuh"
 
 namespace gbs {
 
@@ -42,21 +43,6 @@ struct MergeArgs {
   int P;
   long long D;
 };
-
-// Largest i in [0, n] with rowptr[i] + i <= d (rows finished at merge
-// diagonal d).
-__device__ __forceinline__ int merge_search(const int *__restrict__ rowptr, int n, int nnz,
-                                            long long d) {
-  long long lo = d - nnz;
-  if (lo < 0) lo = 0;
-  long long hi = d < n ? d : n;
-  while (lo < hi) {
-    long long mid = (lo + hi + 1) >> 1;
-    if ((long long)__ldg(rowptr + mid) + mid <= d) lo = mid;
-    else hi = mid - 1;
-  }
-  return (int)lo;
-}
 
 template <int DT, int VEC, int LPR, int CH, int U>
 struct MergeKernel {

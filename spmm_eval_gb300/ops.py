@@ -267,3 +267,71 @@ def bmm32_bin(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, m: int, n: int
     """Mirror of BMM32_BIN (or BMM32S_BIN with s_layout=True)."""
     _lib.call("gbs_bmm32s_bin" if s_layout else "gbs_bmm32_bin", _ptr(A), _ptr(B), _ptr(C_), m, n, k,
               _stream(A.device))
+
+
+# ---------------------------------------------------------------------------
+# Backward: cached transpose, A^T dC, SDDMM
+# ---------------------------------------------------------------------------
+class CSRTranspose:
+    """A^T of a CSR pattern (device arrays owned by the library handle)."""
+
+    def __init__(self, A: CSR):
+        A.validate_layout()
+        self.nrows, self.ncols, self.nnz = A.nrows, A.ncols, A.nnz
+        self.device = A.rowptr.device
+        h = C.c_void_p()
+        _lib.call("gbs_csr_transpose_create", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
+                  _stream(self.device), C.byref(h))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbs_csr_transpose_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def arrays(self):
+        """(t_rowptr, t_colind, perm) copied into new torch tensors."""
+        rp = torch.empty(self.ncols + 1, dtype=torch.int32, device=self.device)
+        ci = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=self.device)
+        pm = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=self.device)
+        _lib.call("gbs_csr_transpose_copy", self._h, _ptr(rp), _ptr(ci), _ptr(pm), _stream(self.device))
+        return rp, ci[: self.nnz], pm[: self.nnz]
+
+    def values(self, vals: torch.Tensor) -> torch.Tensor:
+        _check_cuda("vals", vals, torch.float32)
+        out = torch.empty_like(vals)
+        _lib.call("gbs_csr_transpose_values", self._h, _ptr(vals), _ptr(out), _stream(self.device))
+        return out
+
+    def spmm(self, t_vals: torch.Tensor | None, dC: torch.Tensor, out: torch.Tensor | None = None,
+             workspace: SpmmWorkspace | None = None) -> torch.Tensor:
+        """dB = A^T dC (FP32 out)."""
+        _check_cuda("dC", dC, tuple(_DT))
+        F = int(dC.shape[1])
+        if out is None:
+            out = torch.empty((self.ncols, F), dtype=torch.float32, device=dC.device)
+        ws = workspace or SpmmWorkspace()
+        nbytes = spmm_workspace_bytes(self.ncols, self.nnz, F, dC.dtype)
+        buf = ws.get(nbytes, dC.device)
+        _lib.call("gbs_csr_spmm_transposed", self._h, _ptr(t_vals), _ptr(dC), _DT[dC.dtype], F, _ptr(out),
+                  _ptr(buf), buf.numel(), _stream(dC.device))
+        return out
+
+
+def sddmm(A: CSR, G: torch.Tensor, H: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """out[e] = <G[row(e)], H[col(e)]> on A's pattern (FP32)."""
+    A.validate_layout()
+    _check_cuda("G", G, tuple(_DT))
+    _check_cuda("H", H, tuple(_DT))
+    if G.dtype != H.dtype:
+        raise TypeError("G and H must have the same dtype")
+    F = int(G.shape[1])
+    if out is None:
+        out = torch.empty(A.nnz, dtype=torch.float32, device=G.device)
+    _lib.call("gbs_sddmm", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind), _ptr(G), _ptr(H),
+              _DT[G.dtype], F, _ptr(out), _stream(G.device))
+    return out
