@@ -119,6 +119,11 @@ def make_inputs(device):
     return g, B
 
 
+def make_grad(shape, device):
+    from spmm_eval_gb300 import graphs as G
+    return G.normal(0x5EED + 5, 11, tuple(shape), device=device)
+
+
 def sample_rows_for_error(g, k=192):
     import torch
     deg = (g.rowptr[1:] - g.rowptr[:-1]).to("cpu")
@@ -300,6 +305,30 @@ def run_ours(args):
     ms_f32 = max_over_ranks(ms_f32, world, dev)
     ms_bf16 = sum(timed(step_bf16, args.steps, "timed_bf16")) / args.steps
 
+    # forward + backward of Y = A H: fwd SpMM, bwd A^T dY (cached transpose)
+    # and SDDMM for d(values); FP32 vs BF16 features (H, dY), FP32 accumulate
+    T = ops.CSRTranspose(ops.CSR(g.rowptr, g.colind, None, n, n))
+    t_vals = T.values(g.vals)
+    Gd = make_grad(B.shape, dev)
+    Gh = Gd.to(torch.bfloat16)
+    dH = torch.empty_like(C)
+    dvals = torch.empty_like(g.vals)
+    Apat = ops.CSR(g.rowptr, g.colind, None, n, n)
+
+    def fwd_bwd(Hx, Gx, Cx):
+        ops.csr_spmm(A, Hx, out=Cx, workspace=ws)
+        T.spmm(t_vals, Gx, out=dH, workspace=ws)
+        ops.sddmm(Apat, Gx, Hx, out=dvals)
+
+    for _ in range(3):
+        fwd_bwd(B, Gd, C)
+        fwd_bwd(Bh, Gh, Ch)
+    torch.cuda.synchronize(dev)
+    fb_steps = max(3, min(args.steps, 20))
+    ms_fb32 = sum(timed(lambda: fwd_bwd(B, Gd, C), fb_steps, "timed_fwdbwd_f32")) / fb_steps
+    ms_fb16 = sum(timed(lambda: fwd_bwd(Bh, Gh, Ch), fb_steps, "timed_fwdbwd_bf16")) / fb_steps
+    del Gd, Gh
+
     bytes_f32 = gather_bytes(n, nnz, F, 4)
     bytes_bf16 = gather_bytes(n, nnz, F, 2)
     value = world * bytes_f32 / (ms_f32 * 1e-3) / 1e9
@@ -360,6 +389,9 @@ def run_ours(args):
                      "traffic": traffic, "peak_source": peak_kind,
                      "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per launch",
                      "bytes_per_launch": bytes_f32},
+        "fwd_bwd": {"what": "SpMM A H + SpMM A^T dY + SDDMM(dY, H), F=256",
+                    "f32_ms": round(ms_fb32, 4), "bf16_ms": round(ms_fb16, 4),
+                    "bf16_speedup": round(ms_fb32 / ms_fb16, 3)},
         "bf16": {"ms_per_step": round(ms_bf16, 4),
                  "gbs_gather_model": round(bytes_bf16 / (ms_bf16 * 1e-3) / 1e9, 1),
                  "speedup_vs_f32": round(ms_f32 / ms_bf16, 3)},

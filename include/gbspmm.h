@@ -54,6 +54,24 @@ GBS_API const char *gbs_last_error(void);
 GBS_API int gbs_abi_version(void);
 
 /* ------------------------------------------------------------------------
+ * Matrix Market ingest (host).  Same result as readMtx<float>(...,
+ * directed = 0, ...) + coo2csr in the reference (test_spmm_full.cu:99-113,
+ * backend/readMtx.hpp:351-422, :246-304): 0-based, sorted by (row, col),
+ * duplicates kept, symmetric files not expanded, pattern values 1.0.
+ * Errors (not undefined state) for truncated files, out-of-range indices,
+ * complex or dense files.
+ * ------------------------------------------------------------------------ */
+typedef struct gbs_host_csr {
+  int nrows, ncols, nnz;
+  int *rowptr;  /* nrows + 1 */
+  int *colind;  /* nnz */
+  float *vals;  /* nnz */
+} gbs_host_csr;
+
+GBS_API gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out);
+GBS_API void gbs_host_csr_free(gbs_host_csr *csr);
+
+/* ------------------------------------------------------------------------
  * CSR SpMM  C = A * B   (A: nrows x ncols CSR, B: ncols x F, C: nrows x F)
  *
  * Replaces the cuSPARSE call of evalCSRSpmmFloatCuSPARSE

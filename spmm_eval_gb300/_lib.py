@@ -31,10 +31,18 @@ st = C.c_int  # gbs_status
 pi32 = C.POINTER(C.c_int)
 psz = C.POINTER(C.c_size_t)
 
+class HostCSR(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("nnz", C.c_int),
+                ("rowptr", C.POINTER(C.c_int)), ("colind", C.POINTER(C.c_int)),
+                ("vals", C.POINTER(C.c_float))]
+
+
 # name -> (restype, argtypes); every entry point declared in include/gbspmm.h
 SIGNATURES: dict[str, tuple] = {
     "gbs_last_error": (C.c_char_p, []),
     "gbs_abi_version": (C.c_int, []),
+    "gbs_mtx_read": (st, [C.c_char_p, C.POINTER(HostCSR)]),
+    "gbs_host_csr_free": (None, [C.POINTER(HostCSR)]),
     "gbs_csr_spmm_workspace_size": (st, [i32, i32, i32, i32, psz]),
     "gbs_csr_spmm_workspace_init": (st, [p, sz, p]),
     "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),

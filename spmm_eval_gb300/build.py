@@ -65,7 +65,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     """Compile csrc/*.cu and link lib/libgbspmm.so; returns the library path."""
     BUILD.mkdir(parents=True, exist_ok=True)
     LIBDIR.mkdir(parents=True, exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     hdr = _newest_header()
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
@@ -84,5 +84,40 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
+APPS = PKG / "apps"
+BIN = PKG / "bin"
+# {kernel_name} executables of the reference's driver surface, all links to
+# one binary that dispatches on its program name
+DRIVER_NAMES = ["spmmfbf", "spmmcsr", "spmmcsr_bf16", "spmmb2sr8", "spmmb2sr16", "spmmb2sr32", "spmmbmm"]
+
+
+def build_apps(verbose: bool = False) -> Path:
+    """Compile apps/spmm_driver.cu into bin/spmm_driver (linked against
+    lib/libgbspmm.so and cuSPARSE, the reference's verifier) and the
+    per-kernel links."""
+    lib = build(verbose)
+    BIN.mkdir(parents=True, exist_ok=True)
+    exe = BIN / "spmm_driver"
+    src = APPS / "spmm_driver.cu"
+    newest = max(src.stat().st_mtime, lib.stat().st_mtime, _newest_header())
+    if not exe.exists() or exe.stat().st_mtime < newest:
+        cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", f"-I{INCLUDE}", str(src), "-o", str(exe),
+               f"-L{LIBDIR}", "-lgbspmm", "-lcusparse", "-Xlinker", "-rpath,$ORIGIN/../lib"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    for name in DRIVER_NAMES:
+        link = BIN / name
+        if not link.is_symlink():
+            if link.exists():
+                link.unlink()
+            link.symlink_to("spmm_driver")
+    return exe
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
+    if "--apps" in sys.argv:
+        print(build_apps(verbose="-v" in sys.argv))

@@ -1,0 +1,195 @@
+// Matrix Market (.mtx) -> host CSR with the reference's ingest semantics:
+// readMtx<float>(..., directed = 0, ...) followed by coo2csr
+// (test_spmm_full.cu:99-113, backend/readMtx.hpp:351-422, :246-304,
+// backend/mmio.hpp:128-228):
+//   * banner "%%MatrixMarket matrix coordinate <real|integer|pattern>
+//     <general|symmetric|hermitian|skew-symmetric>", fields
+//     case-insensitive;
+//   * comment lines start with '%'; the size line is the first other line
+//     (if it does not hold three integers, integers are read on until three
+//     are found, as mm_read_mtx_crd_size does);
+//   * entries are 1-based "row col [value]"; pattern entries get 1.0,
+//     integer values are read as integers, real values as float;
+//   * no symmetrisation and no removal of duplicates or self-loops (the
+//     reference's removeSelfloop call is commented out, readMtx.hpp:413): a
+//     symmetric file yields only the listed triangle;
+//   * entries sorted by (row, col); entries with equal (row, col) keep file
+//     order (the reference's std::sort leaves their order unspecified).
+// Unlike the reference, a truncated file, an index outside the stated size,
+// a complex or dense ("array") file is an error instead of undefined state.
+#include <algorithm>
+#include <cctype>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+struct Reader {
+  std::vector<char> buf;
+  size_t pos = 0;
+
+  bool load(const char *path) {
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return false;
+    std::fseek(f, 0, SEEK_END);
+    long n = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (n < 0) {
+      std::fclose(f);
+      return false;
+    }
+    buf.resize((size_t)n + 1);
+    size_t got = n > 0 ? std::fread(buf.data(), 1, (size_t)n, f) : 0;
+    std::fclose(f);
+    buf.resize(got + 1);
+    buf[got] = '\0';
+    return true;
+  }
+  bool eof() const { return pos + 1 >= buf.size(); }
+  // next line without the newline; false at end of file
+  bool line(std::string *out) {
+    if (eof()) return false;
+    size_t s = pos;
+    while (pos + 1 < buf.size() && buf[pos] != '\n') ++pos;
+    out->assign(buf.data() + s, pos - s);
+    if (pos + 1 < buf.size()) ++pos;
+    if (!out->empty() && out->back() == '\r') out->pop_back();
+    return true;
+  }
+  void skip_ws() {
+    while (pos + 1 < buf.size() && std::isspace((unsigned char)buf[pos])) ++pos;
+  }
+  bool read_long(long *v) {
+    skip_ws();
+    if (eof()) return false;
+    char *end = nullptr;
+    errno = 0;
+    long x = std::strtol(buf.data() + pos, &end, 10);
+    if (end == buf.data() + pos) return false;
+    pos = (size_t)(end - buf.data());
+    *v = x;
+    return true;
+  }
+  bool read_float(float *v) {
+    skip_ws();
+    if (eof()) return false;
+    char *end = nullptr;
+    float x = std::strtof(buf.data() + pos, &end);
+    if (end == buf.data() + pos) return false;
+    pos = (size_t)(end - buf.data());
+    *v = x;
+    return true;
+  }
+};
+
+std::string lower(std::string s) {
+  for (auto &c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+
+}  // namespace
+
+using namespace gbs;
+
+extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
+  clear_error();
+  GBS_REQUIRE(path && out, "mtx: null argument");
+  std::memset(out, 0, sizeof(*out));
+  Reader rd;
+  if (!rd.load(path)) return fail(GBS_ERR_INVALID_ARG, std::string("mtx: cannot open ") + path);
+  std::string ln;
+  if (!rd.line(&ln)) return fail(GBS_ERR_INVALID_ARG, "mtx: empty file");
+  char banner[64] = {0}, mtx[64] = {0}, crd[64] = {0}, dtype[64] = {0}, sym[64] = {0};
+  if (std::sscanf(ln.c_str(), "%63s %63s %63s %63s %63s", banner, mtx, crd, dtype, sym) != 5)
+    return fail(GBS_ERR_INVALID_ARG, "mtx: banner needs 5 fields");
+  if (std::strncmp(banner, "%%MatrixMarket", 14) != 0) return fail(GBS_ERR_INVALID_ARG, "mtx: no %%MatrixMarket banner");
+  const std::string m = lower(mtx), c = lower(crd), d = lower(dtype), y = lower(sym);
+  if (m != "matrix") return fail(GBS_ERR_UNSUPPORTED, "mtx: object must be 'matrix'");
+  if (c != "coordinate") return fail(GBS_ERR_UNSUPPORTED, "mtx: only coordinate (sparse) files are supported");
+  int kind;  // 0 real, 1 integer, 2 pattern
+  if (d == "real") kind = 0;
+  else if (d == "integer") kind = 1;
+  else if (d == "pattern") kind = 2;
+  else return fail(GBS_ERR_UNSUPPORTED, "mtx: data type must be real, integer or pattern");
+  if (y != "general" && y != "symmetric" && y != "hermitian" && y != "skew-symmetric")
+    return fail(GBS_ERR_UNSUPPORTED, "mtx: unknown symmetry field");
+
+  long M = 0, N = 0, NZ = 0;
+  bool have = false;
+  while (rd.line(&ln)) {
+    if (!ln.empty() && ln[0] == '%') continue;
+    if (std::sscanf(ln.c_str(), "%ld %ld %ld", &M, &N, &NZ) == 3) have = true;
+    break;
+  }
+  if (!have) {  // mm_read_mtx_crd_size: keep reading integers until 3
+    if (!(rd.read_long(&M) && rd.read_long(&N) && rd.read_long(&NZ)))
+      return fail(GBS_ERR_INVALID_ARG, "mtx: missing size line");
+  }
+  if (M < 0 || N < 0 || NZ < 0 || M > 0x7fffffffL || N > 0x7fffffffL || NZ > 0x7fffffffL)
+    return fail(GBS_ERR_INVALID_ARG, "mtx: size out of range");
+
+  std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
+  std::vector<float> v((size_t)NZ);
+  for (long e = 0; e < NZ; ++e) {
+    long r, cc;
+    if (!rd.read_long(&r) || !rd.read_long(&cc))
+      return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
+    float val = 1.0f;
+    if (kind == 0) {
+      if (!rd.read_float(&val)) return fail(GBS_ERR_INVALID_ARG, "mtx: missing value");
+    } else if (kind == 1) {
+      long iv;
+      if (!rd.read_long(&iv)) return fail(GBS_ERR_INVALID_ARG, "mtx: missing value");
+      val = (float)(int)iv;
+    }
+    if (r < 1 || r > M || cc < 1 || cc > N)
+      return fail(GBS_ERR_INVALID_ARG, "mtx: entry " + std::to_string(e + 1) + " outside the matrix");
+    ri[(size_t)e] = (int)(r - 1);
+    ci[(size_t)e] = (int)(cc - 1);
+    v[(size_t)e] = val;
+  }
+
+  // counting sort by row (stable), then stable sort of each row by column
+  std::vector<int> rowptr((size_t)M + 1, 0);
+  for (long e = 0; e < NZ; ++e) rowptr[(size_t)ri[(size_t)e] + 1]++;
+  for (long i = 0; i < M; ++i) rowptr[(size_t)i + 1] += rowptr[(size_t)i];
+  std::vector<int> order((size_t)NZ), fill(rowptr.begin(), rowptr.end() - 1);
+  for (long e = 0; e < NZ; ++e) order[(size_t)fill[(size_t)ri[(size_t)e]]++] = (int)e;
+  for (long i = 0; i < M; ++i)
+    std::stable_sort(order.begin() + rowptr[(size_t)i], order.begin() + rowptr[(size_t)i + 1],
+                     [&](int a, int b) { return ci[(size_t)a] < ci[(size_t)b]; });
+
+  out->nrows = (int)M;
+  out->ncols = (int)N;
+  out->nnz = (int)NZ;
+  out->rowptr = (int *)std::malloc(sizeof(int) * ((size_t)M + 1));
+  out->colind = (int *)std::malloc(sizeof(int) * (size_t)(NZ > 0 ? NZ : 1));
+  out->vals = (float *)std::malloc(sizeof(float) * (size_t)(NZ > 0 ? NZ : 1));
+  if (!out->rowptr || !out->colind || !out->vals) {
+    gbs_host_csr_free(out);
+    return fail(GBS_ERR_OOM, "mtx: host allocation failed");
+  }
+  std::memcpy(out->rowptr, rowptr.data(), sizeof(int) * ((size_t)M + 1));
+  for (long e = 0; e < NZ; ++e) {
+    const int k = order[(size_t)e];
+    out->colind[e] = ci[(size_t)k];
+    out->vals[e] = v[(size_t)k];
+  }
+  return GBS_OK;
+}
+
+extern "C" void gbs_host_csr_free(gbs_host_csr *c) {
+  if (!c) return;
+  std::free(c->rowptr);
+  std::free(c->colind);
+  std::free(c->vals);
+  c->rowptr = nullptr;
+  c->colind = nullptr;
+  c->vals = nullptr;
+}

@@ -23,8 +23,8 @@ struct SddmmArgs {
   long long D;
 };
 
-template <int DT, int VEC, int LPR, int CH, int U>
-__global__ void __launch_bounds__(256) k_sddmm(SddmmArgs a) {
+template <int DT, int VEC, int LPR, int CH, int U, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_sddmm(SddmmArgs a) {
   constexpr int NSUB = 32 / LPR;
   constexpr int KPS = LPR;
   using F_ = Feat<DT, VEC>;
@@ -100,9 +100,12 @@ struct SVar {
 
 template <int DT, int VEC, int LPR, int CH>
 SVar mks() {
-  constexpr int UCAP = CH >= 8 ? 1 : 8 / CH;
+  constexpr int UCAP = CH == 1 ? 4 : (CH == 2 ? 2 : 1);
   constexpr int U = UCAP < LPR ? UCAP : LPR;
-  return SVar{(const void *)&k_sddmm<DT, VEC, LPR, CH, U>, VEC};
+  // register estimate: accumulators (+ blocked partials) + loads in flight
+  constexpr int EST = 24 + 2 * CH * VEC + U * CH * 4 + U;
+  constexpr int MINB = EST <= 64 ? 4 : (EST <= 80 ? 3 : (EST <= 128 ? 2 : 1));
+  return SVar{(const void *)&k_sddmm<DT, VEC, LPR, CH, U, MINB>, VEC};
 }
 
 template <int DT, int VEC>

@@ -335,3 +335,22 @@ def sddmm(A: CSR, G: torch.Tensor, H: torch.Tensor, out: torch.Tensor | None = N
     _lib.call("gbs_sddmm", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind), _ptr(G), _ptr(H),
               _DT[G.dtype], F, _ptr(out), _stream(G.device))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Matrix Market ingest (host)
+# ---------------------------------------------------------------------------
+def read_mtx(path: str):
+    """(nrows, ncols, rowptr, colind, vals) as numpy arrays, with the
+    reference's readMtx + coo2csr semantics."""
+    import numpy as np
+    h = _lib.HostCSR()
+    _lib.call("gbs_mtx_read", str(path).encode(), C.byref(h))
+    try:
+        n, nnz = h.nrows, h.nnz
+        rowptr = np.ctypeslib.as_array(h.rowptr, shape=(n + 1,)).copy()
+        colind = np.ctypeslib.as_array(h.colind, shape=(max(nnz, 1),))[:nnz].copy()
+        vals = np.ctypeslib.as_array(h.vals, shape=(max(nnz, 1),))[:nnz].copy()
+        return h.nrows, h.ncols, rowptr, colind, vals
+    finally:
+        _lib.load().gbs_host_csr_free(C.byref(h))
