@@ -78,16 +78,20 @@ struct MergeKernel {
       for (int c = 0; c < CH; ++c)
 #pragma unroll
         for (int q = 0; q < VEC; ++q) bs[c][q] = 0.f;
-      for (int u0 = 0; u0 < KPS; u0 += U) {
-        if (u0 * NSUB >= n_valid) break;
+      // rounds of U nonzeros per sub-group; a runtime trip count (not an
+      // unrolled loop with early exits) keeps the loads of one round together
+      const int rounds = (n_valid + U * NSUB - 1) / (U * NSUB);
+#pragma unroll 1
+      for (int rd = 0; rd < rounds; ++rd) {
+        const int u0 = rd * U;
         raw bv[U][CH];
         float vv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int k = (u0 + u) * NSUB + sub;
+          const int k = ((u0 + u) * NSUB + sub) & 31;
           const int col = __shfl_sync(0xffffffffu, my_col, k);
           const float v = __shfl_sync(0xffffffffu, my_val, k);
-          const bool ok = k < n_valid;
+          const bool ok = (u0 + u) * NSUB + sub < n_valid;
           vv[u] = ok ? v : 0.f;
           const size_t rowbase = (size_t)col * (size_t)a.ldb;
 #pragma unroll
