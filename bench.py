@@ -411,35 +411,78 @@ def run_ours(args):
 
 
 def run_profile_case(args):
-    """Small fixed launch sequence for ncu: generate, free the generator's
-    cached memory, 2 warm-up launches, then `--steps` launches of the FP32
-    SpMM (and the same of BF16).  `full` is the bench graph; `eighth` keeps
-    the 232,965 nodes (B stays larger than L2) with 1/8 of the degree."""
+    """Short fixed launch sequences for ncu (2 warm-up launches, then
+    `--steps` launches of each kernel, nothing else heavy):
+      full   : bench graph, FP32 then BF16 merge-path SpMM, F = 256
+      eighth : same nodes (B still larger than L2), 1/8 of the degree
+      fwdbwd : eighth graph, SpMM + A^T SpMM + SDDMM (FP32, then BF16)
+      b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
+               B2SR BMM F = 256
+      bmm    : 4096^3 binary GEMM, popc then mma .b1 (XOR counts)"""
     import torch
     from spmm_eval_gb300 import graphs as G
     from spmm_eval_gb300 import ops
     dev = torch.device("cuda:0")
-    if args.profile_case == "full":
-        g = G.gcn_normalize(G.reddit_like(device=dev))
-    else:
-        g = G.gcn_normalize(G.chung_lu(232_965, 1.8, 59.9 / 8, 20_000.0 / 8, 0x5EED + 4, dev,
-                                       "reddit_like_eighth"))
-    B = G.normal(0x5EED + 4, 9, (g.ncols, 256), device=dev)
-    Bh = B.to(torch.bfloat16)
+    case = args.profile_case
+    out = {"profile_case": case}
+    if case in ("full", "eighth", "fwdbwd"):
+        if case == "full":
+            g = G.gcn_normalize(G.reddit_like(device=dev))
+        else:
+            g = G.gcn_normalize(G.chung_lu(232_965, 1.8, 59.9 / 8, 20_000.0 / 8, 0x5EED + 4, dev,
+                                           "reddit_like_eighth"))
+        B = G.normal(0x5EED + 4, 9, (g.ncols, 256), device=dev)
+        Bh = B.to(torch.bfloat16)
+        A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
+        C = torch.empty((g.nrows, 256), device=dev)
+        ws = ops.SpmmWorkspace()
+        if case == "fwdbwd":
+            T = ops.CSRTranspose(ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols))
+            tv = T.values(g.vals)
+            Gd = G.normal(0x5EED + 5, 11, (g.nrows, 256), device=dev)
+            Gh = Gd.to(torch.bfloat16)
+            dH = torch.empty_like(C)
+            dv = torch.empty_like(g.vals)
+            Ap = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            for Hx, Gx in ((B, Gd), (Bh, Gh)):
+                for _ in range(2 + args.steps):
+                    ops.csr_spmm(A, Hx, out=C, workspace=ws)
+                    T.spmm(tv, Gx, out=dH, workspace=ws)
+                    ops.sddmm(Ap, Gx, Hx, out=dv)
+        else:
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            for Bx in (B, Bh):
+                for _ in range(2 + args.steps):
+                    ops.csr_spmm(A, Bx, out=C, workspace=ws)
+        out.update(nodes=g.nrows, nnz=g.nnz)
+    elif case == "b2sr":
+        g = G.flickr_like(device=dev)
+        A = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
+        B = G.normal(3, 3, (g.ncols, 256), device=dev)
+        Xw = ops.pack_sign_rows(B)
+        for _ in range(2 + args.steps):
+            Ab = ops.csr2b2sr(A, 4)
+        for _ in range(2 + args.steps):
+            ops.b2sr_spmm(Ab, B)
+        for _ in range(2 + args.steps):
+            ops.b2sr_bmm(Ab, Xw, 256)
+        out.update(nodes=g.nrows, nnz=g.nnz, nnzb=Ab.nnzb)
+    elif case == "bmm":
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(0)
+        Kw, M = 128, 4096
+        Aw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
+        Bw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
+        Co = torch.empty((M, M), dtype=torch.int32, device=dev)
+        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA):
+            for _ in range(2 + args.steps):
+                ops.bmm_b1(Aw, Bw, ops.BMM_XOR, algo, out=Co)
     torch.cuda.synchronize()
-    torch.cuda.empty_cache()
-    A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
-    C = torch.empty((g.nrows, 256), device=dev)
-    ws = ops.SpmmWorkspace()
-    for _ in range(2):
-        ops.csr_spmm(A, B, out=C, workspace=ws)
-    for _ in range(args.steps):
-        ops.csr_spmm(A, B, out=C, workspace=ws)
-    for _ in range(args.steps):
-        ops.csr_spmm(A, Bh, out=C, workspace=ws)
-    torch.cuda.synchronize()
-    print(json.dumps({"profile_case": args.profile_case, "nodes": g.nrows, "nnz": g.nnz,
-                      "device_bytes": torch.cuda.max_memory_allocated()}))
+    out["device_bytes"] = torch.cuda.max_memory_allocated()
+    print(json.dumps(out))
 
 
 def main():
@@ -449,7 +492,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["full", "eighth"], default=None,
+    ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "b2sr", "bmm"], default=None,
                     help="run a short fixed launch sequence for ncu instead of the bench")
     args = ap.parse_args()
     if args.profile_case:
