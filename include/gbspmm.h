@@ -89,9 +89,11 @@ GBS_API void gbs_host_csr_free(gbs_host_csr *csr);
  * ------------------------------------------------------------------------ */
 
 /* Bytes of workspace gbs_csr_spmm / gbs_csr_spmm_cb need for this shape on
- * the current device (any alignment, any column block).  The workspace must be zero-filled before its first use
- * (gbs_csr_spmm_workspace_init); every call leaves it zero-filled again.
- * A workspace must not be used by two calls that can overlap on the GPU. */
+ * the current device (any alignment, any column block).  The workspace must
+ * be zero-filled before its first use (gbs_csr_spmm_workspace_init); its
+ * arrival counters are back to zero after every call, so one workspace can
+ * serve calls of any shape in sequence.  It must not be used by two calls
+ * that can overlap on the GPU. */
 GBS_API gbs_status gbs_csr_spmm_workspace_size(int nrows, int nnz, int F,
                                        gbs_dtype btype, size_t *bytes);
 GBS_API gbs_status gbs_csr_spmm_workspace_init(void *d_workspace, size_t bytes,
@@ -112,6 +114,16 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
                            const void *d_B, gbs_dtype btype, int F, int col_block,
                            float *d_C, void *d_workspace, size_t workspace_bytes,
                            gbs_stream_t stream);
+
+/* Host-buffer form for callers that hold A, B and C in host memory, as the
+ * reference's evalCSRSpmmFloatCuSPARSE does (test_spmm_full.cu:212-342):
+ * copies in, C = A * B, copies out, and returns when h_C is filled.  A is
+ * sent in row ranges of ~nnz/8 nonzeros so the copies overlap the kernels
+ * (pinned host buffers are needed for the overlap; pageable ones work,
+ * serialised).  Allocates its device buffers stream-ordered on `stream`. */
+GBS_API gbs_status gbs_csr_spmm_host(int nrows, int ncols, int nnz, const int *h_rowptr,
+                             const int *h_colind, const float *h_vals, const void *h_B,
+                             gbs_dtype btype, int F, float *h_C, gbs_stream_t stream);
 
 /* One-call FP32 form with the argument meaning of the cuSPARSE generic
  * SpMM used by the reference (alpha = 1, beta = 0, FP32 everywhere).

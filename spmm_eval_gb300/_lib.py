@@ -48,6 +48,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_cb": (st, [i32, i32, i32, p, p, p, p, i32, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_f32": (st, [i32, i32, i32, p, p, p, p, i32, p, p]),
+    "gbs_csr_spmm_host": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr_spmm_noalloc": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr_transpose_create": (st, [i32, i32, i32, p, p, p, C.POINTER(p)]),
     "gbs_csr_transpose_arrays": (st, [p, C.POINTER(p), C.POINTER(p), C.POINTER(p)]),

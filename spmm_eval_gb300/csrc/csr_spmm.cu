@@ -32,7 +32,8 @@ struct MergeArgs {
   int F;     // width of the column block handled by this launch
   int nvec;  // F / VEC
   long long ldb, ldc;  // row strides of B and C (elements)
-  const int *rowptr;
+  const int *rowptr;  // rowptr[0] == rp_base; colind/vals point at entry rp_base
+  int rp_base;
   const int *colind;
   const float *vals;  // may be null: binary A
   const void *B;
@@ -135,7 +136,7 @@ struct MergeKernel {
   // written that piece to its head or tail slot.  The last of the (w2 - w1 + 1) contributors sums the
   // pieces in warp order and writes C.
   static __device__ __forceinline__ void finish_split(const MergeArgs &a, int r, int lane) {
-    const int rb = __ldg(a.rowptr + r), re = __ldg(a.rowptr + r + 1);
+    const int rb = __ldg(a.rowptr + r) - a.rp_base, re = __ldg(a.rowptr + r + 1) - a.rp_base;
     const int w1 = (int)(((long long)rb + r) / a.D);
     const int w2 = (int)(((long long)re + r) / a.D);
     __threadfence();
@@ -175,14 +176,14 @@ struct MergeKernel {
     const long long d0 = min((long long)warp * a.D, total);
     const long long d1 = min((long long)(warp + 1) * a.D, total);
     if (d0 >= d1) return;
-    const int i0 = merge_search(a.rowptr, a.nrows, a.nnz, d0);
-    const int i1 = merge_search(a.rowptr, a.nrows, a.nnz, d1);
+    const int i0 = merge_search(a.rowptr, a.nrows, a.nnz, d0, a.rp_base);
+    const int i1 = merge_search(a.rowptr, a.nrows, a.nnz, d1, a.rp_base);
     int j = (int)(d0 - i0);
     const int j1 = (int)(d1 - i1);
 
     float acc[CH][VEC];
     for (int r = i0; r < i1; ++r) {
-      const int rb = __ldg(a.rowptr + r), re = __ldg(a.rowptr + r + 1);
+      const int rb = __ldg(a.rowptr + r) - a.rp_base, re = __ldg(a.rowptr + r + 1) - a.rp_base;
       accumulate(a, j, re, lane, acc);
       if (j == rb) {
         write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
@@ -289,9 +290,23 @@ gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out) {
   return GBS_OK;
 }
 
+// Workspace layout: [arrival counters][partial-sum slots].  The counter
+// region has a fixed size on a device (one int per warp the device can hold
+// resident), so every call finds its counters at the same place whatever
+// its shape, and that region is only ever written as counters: each call
+// leaves it zero, and a workspace reused across shapes stays valid.  The
+// slot region (2 P rows of the column-block width) needs no initialisation.
+size_t spmm_counter_bytes() {
+  DeviceInfo di;
+  int warps = 152 * 64;
+  if (device_info(&di) == GBS_OK) warps = di.sm_count * (di.max_threads_per_sm / 32);
+  else clear_error();
+  return align_up((size_t)warps * sizeof(int), 256);
+}
+
 size_t spmm_workspace_bytes(int P, int Fw) {
   const size_t ldp = align_up((size_t)Fw, 4);
-  return align_up((size_t)2 * P * ldp * sizeof(float), 256) + align_up((size_t)P * sizeof(int), 256);
+  return spmm_counter_bytes() + align_up((size_t)2 * P * ldp * sizeof(float), 256);
 }
 
 // Column-block width.  col_block > 0 forces F / col_block launches of
@@ -318,8 +333,9 @@ gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col
 
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
-                       float *C, long long ldc, void *ws, cudaStream_t stream) {
+                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base) {
   MergeArgs a;
+  a.rp_base = rp_base;
   a.nrows = nrows;
   a.nnz = nnz;
   a.F = Fw;
@@ -336,9 +352,8 @@ gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const in
   const long long total = (long long)nrows + nnz;
   a.D = (total + P - 1) / P;
   if (a.D < 1) a.D = 1;
-  a.partials = reinterpret_cast<float *>(ws);
-  a.counters = reinterpret_cast<int *>(reinterpret_cast<char *>(ws) +
-                                       align_up((size_t)2 * P * a.ldp * sizeof(float), 256));
+  a.counters = reinterpret_cast<int *>(ws);
+  a.partials = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + spmm_counter_bytes());
   const int blocks = (P * 32 + kThreads - 1) / kThreads;
   void *args[] = {&a};
   GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(kThreads), args, 0, stream));
@@ -394,11 +409,11 @@ gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes
 
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, int rp_base) {
   for (int b = 0; b < p.nblk; ++b) {
     const char *Bb = reinterpret_cast<const char *>(B) + (size_t)b * p.Fw * p.esize;
     GBS_TRY(spmm_launch(p.v, p.P, nrows, nnz, rowptr, colind, vals, Bb, F, p.Fw,
-                        C + (size_t)b * p.Fw, F, ws, stream));
+                        C + (size_t)b * p.Fw, F, ws, stream, rp_base));
   }
   return GBS_OK;
 }

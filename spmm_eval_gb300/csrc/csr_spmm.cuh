@@ -23,6 +23,7 @@ struct SpmmPlan {
 
 gbs_status spmm_select(int dt, int Fw, bool vec16, SpmmVariant *out);
 gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out);
+size_t spmm_counter_bytes();
 size_t spmm_workspace_bytes(int P, int Fw);
 gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes);
 gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
@@ -31,9 +32,9 @@ gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B
                      int col_block, SpmmPlan *p);
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
-                       float *C, long long ldc, void *ws, cudaStream_t stream);
+                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base = 0);
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream);
+                    cudaStream_t stream, int rp_base = 0);
 
 }  // namespace gbs

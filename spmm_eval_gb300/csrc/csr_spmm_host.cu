@@ -1,0 +1,156 @@
+// CSR SpMM from host buffers, pipelined: the call a host-side caller of
+// evalCSRSpmmFloatCuSPARSE (test_spmm_full.cu:212-342) makes -- host CSR and
+// host B in, host C out -- with the copies overlapped with the kernels.
+//
+// B goes to the device first (every row needs it).  A is copied in K row
+// ranges of about nnz/K nonzeros each on a copy stream; the merge-path SpMM
+// of range k starts on the caller's stream as soon as range k and B have
+// arrived, and range k of C is copied back on a third stream as soon as it is
+// computed.  With pinned host buffers the three engines overlap; with
+// pageable buffers the copies are still correct, only serialised.
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "csr_spmm.cuh"
+#include "util.cuh"
+
+namespace gbs {
+namespace {
+
+constexpr int kChunks = 8;
+
+struct StreamPair {
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+};
+
+gbs_status side_streams(StreamPair *out) {
+  static std::mutex mu;
+  static StreamPair per_dev[64];
+  int dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "csr spmm host: device ordinal >= 64");
+  std::lock_guard<std::mutex> lock(mu);
+  StreamPair &p = per_dev[dev];
+  if (!p.h2d) {
+    GBS_CUDA_TRY(cudaStreamCreateWithFlags(&p.h2d, cudaStreamNonBlocking));
+    GBS_CUDA_TRY(cudaStreamCreateWithFlags(&p.d2h, cudaStreamNonBlocking));
+  }
+  *out = p;
+  return GBS_OK;
+}
+
+// Waits for the side streams when the call leaves early on an error, so the
+// device buffers (freed on the caller's stream) are no longer in use.
+struct SideSync {
+  StreamPair sp;
+  ~SideSync() {
+    if (sp.h2d) cudaStreamSynchronize(sp.h2d);
+    if (sp.d2h) cudaStreamSynchronize(sp.d2h);
+  }
+};
+
+struct Events {
+  std::vector<cudaEvent_t> ev;
+  gbs_status make(int n) {
+    ev.resize(n, nullptr);
+    for (auto &e : ev) GBS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return GBS_OK;
+  }
+  ~Events() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" gbs_status gbs_csr_spmm_host(int nrows, int ncols, int nnz, const int *h_rowptr,
+                                        const int *h_colind, const float *h_vals, const void *h_B,
+                                        gbs_dtype btype, int F, float *h_C, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "csr spmm host: bad dtype");
+  GBS_TRY(spmm_check_args(nrows, ncols, nnz, h_rowptr, h_colind, h_B, F, h_C));
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(h_rowptr[0] == 0 && h_rowptr[nrows] == nnz, "csr spmm host: rowptr[0] != 0 or rowptr[n] != nnz");
+  const int dt = btype == GBS_F32 ? 0 : (btype == GBS_BF16 ? 1 : 2);
+  const size_t esz = btype == GBS_F32 ? 4 : 2;
+  cudaStream_t s0 = (cudaStream_t)stream;
+  StreamPair sp;
+  GBS_TRY(side_streams(&sp));
+
+  // row ranges with ~nnz/K nonzeros each
+  std::vector<int> cut{0};
+  for (int k = 1; k < kChunks; ++k) {
+    const long long target = (long long)nnz * k / kChunks;
+    int lo = cut.back(), hi = nrows;
+    while (lo < hi) {  // first row whose start is >= target
+      const int mid = lo + (hi - lo) / 2;
+      if (h_rowptr[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo > cut.back() && lo < nrows) cut.push_back(lo);
+  }
+  cut.push_back(nrows);
+  const int K = (int)cut.size() - 1;
+
+  DevBuf dB, drp, dci, dv, dC;
+  GBS_TRY(dB.alloc((size_t)ncols * F * esz, s0));
+  GBS_TRY(drp.alloc(sizeof(int) * ((size_t)nrows + 1), s0));
+  GBS_TRY(dci.alloc(sizeof(int) * (size_t)nnz, s0));
+  if (h_vals) GBS_TRY(dv.alloc(sizeof(float) * (size_t)nnz, s0));
+  GBS_TRY(dC.alloc(sizeof(float) * (size_t)nrows * F, s0));
+  // plan for the largest range (workspace sized for it, reused by every range)
+  SpmmPlan plan;
+  size_t ws_bytes = 256;
+  for (int k = 0; k < K; ++k) {
+    const int rows = cut[k + 1] - cut[k], nz = h_rowptr[cut[k + 1]] - h_rowptr[cut[k]];
+    GBS_TRY(spmm_plan(dt, rows, ncols, nz, F, dB.p, dC.as<float>(), 0, &plan));
+    if (plan.ws_bytes > ws_bytes) ws_bytes = plan.ws_bytes;
+  }
+  DevBuf ws;
+  GBS_TRY(ws.alloc(ws_bytes, s0));
+  SideSync guard{sp};  // destroyed before the buffers above
+  GBS_CUDA_TRY(cudaMemsetAsync(ws.p, 0, ws_bytes, s0));
+
+  Events ev;
+  GBS_TRY(ev.make(2 + 2 * K + 1));
+  cudaEvent_t ready = ev.ev[0], haveB = ev.ev[1], done = ev.ev[2 + 2 * K];
+  GBS_CUDA_TRY(cudaEventRecord(ready, s0));  // allocations are ordered before the copies
+  GBS_CUDA_TRY(cudaStreamWaitEvent(sp.h2d, ready, 0));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(sp.d2h, ready, 0));
+  GBS_CUDA_TRY(cudaMemcpyAsync(dB.p, h_B, (size_t)ncols * F * esz, cudaMemcpyHostToDevice, sp.h2d));
+  GBS_CUDA_TRY(cudaEventRecord(haveB, sp.h2d));
+  for (int k = 0; k < K; ++k) {
+    const int r0 = cut[k], r1 = cut[k + 1];
+    const int e0 = h_rowptr[r0], e1 = h_rowptr[r1];
+    cudaEvent_t haveA = ev.ev[2 + 2 * k], haveC = ev.ev[3 + 2 * k];
+    GBS_CUDA_TRY(cudaMemcpyAsync(drp.as<int>() + r0, h_rowptr + r0, sizeof(int) * (size_t)(r1 - r0 + 1),
+                                 cudaMemcpyHostToDevice, sp.h2d));
+    if (e1 > e0) {
+      GBS_CUDA_TRY(cudaMemcpyAsync(dci.as<int>() + e0, h_colind + e0, sizeof(int) * (size_t)(e1 - e0),
+                                   cudaMemcpyHostToDevice, sp.h2d));
+      if (h_vals)
+        GBS_CUDA_TRY(cudaMemcpyAsync(dv.as<float>() + e0, h_vals + e0, sizeof(float) * (size_t)(e1 - e0),
+                                     cudaMemcpyHostToDevice, sp.h2d));
+    }
+    GBS_CUDA_TRY(cudaEventRecord(haveA, sp.h2d));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s0, haveA, 0));
+    if (k == 0) GBS_CUDA_TRY(cudaStreamWaitEvent(s0, haveB, 0));
+    GBS_TRY(spmm_plan(dt, r1 - r0, ncols, e1 - e0, F, dB.p, dC.as<float>(), 0, &plan));
+    GBS_TRY(spmm_run(plan, r1 - r0, e1 - e0, drp.as<int>() + r0, dci.as<int>() + e0,
+                     h_vals ? dv.as<float>() + e0 : nullptr, dB.p, F, dC.as<float>() + (size_t)r0 * F, ws.p, s0,
+                     e0));
+    GBS_CUDA_TRY(cudaEventRecord(haveC, s0));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(sp.d2h, haveC, 0));
+    GBS_CUDA_TRY(cudaMemcpyAsync(h_C + (size_t)r0 * F, dC.as<float>() + (size_t)r0 * F,
+                                 sizeof(float) * (size_t)(r1 - r0) * F, cudaMemcpyDeviceToHost, sp.d2h));
+  }
+  GBS_CUDA_TRY(cudaEventRecord(done, sp.d2h));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(s0, done, 0));  // frees below are ordered after all copies
+  GBS_CUDA_TRY(cudaStreamSynchronize(s0));
+  return GBS_OK;
+}

@@ -87,10 +87,8 @@ extern "C" gbs_status gbs_csr_spmm_noalloc(int nrows, int ncols, int nnz, const 
   GBS_TRY(scratch_address(&ws));
   cudaStream_t s = (cudaStream_t)stream;
   // The array keeps whatever the previous call left in it.  Only the arrival
-  // counters must start at zero (partial slots are written before they are
-  // read), so clear exactly that region for this call's layout.
-  const size_t counters_off = align_up((size_t)2 * p.P * align_up((size_t)p.Fw, 4) * sizeof(float), 256);
-  GBS_CUDA_TRY(cudaMemsetAsync(static_cast<char *>(ws) + counters_off, 0,
-                               (size_t)p.P * sizeof(int), s));
+  // counters (the first P ints) must start at zero -- partial slots are
+  // written before they are read -- so clear exactly those.
+  GBS_CUDA_TRY(cudaMemsetAsync(ws, 0, (size_t)p.P * sizeof(int), s));
   return spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
 }

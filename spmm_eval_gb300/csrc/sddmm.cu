@@ -69,20 +69,49 @@ __global__ void __launch_bounds__(256, MINB) k_sddmm(SddmmArgs a) {
               else hv[u][c] = F_::zero();
             }
           }
+          float s[U];
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            float s = 0.f;
+            s[u] = 0.f;
 #pragma unroll
             for (int c = 0; c < CH; ++c) {
               float h[VEC];
               F_::widen(h, hv[u][c]);
 #pragma unroll
-              for (int q = 0; q < VEC; ++q) s = fmaf(g[c][q], h[q], s);
+              for (int q = 0; q < VEC; ++q) s[u] = fmaf(g[c][q], h[q], s[u]);
             }
+          }
+          // Multi-value butterfly over the LPR lanes of the sub-group: each
+          // of the first log2(U) levels halves the values a lane holds (the
+          // lane keeps the half selected by its own offset bit and adds the
+          // partner's copy), the remaining levels finish one value.  Lane sl
+          // ends with the full dot product of nonzero sl / (LPR / U):
+          // (U - 1) + log2(LPR / U) shuffles per U nonzeros instead of
+          // U * log2(LPR).  Fixed order, so deterministic.
+          int nv = U;
 #pragma unroll
-            for (int off = 1; off < LPR; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-            const int k = (u0 + u) * NSUB + sub;
-            if (sl == 0 && k < n_valid) a.out[base + k] = s;
+          for (int off = LPR / 2; off >= 1; off >>= 1) {
+            if (nv > 1) {
+              const int half = nv / 2;
+              const bool upper = (sl & off) != 0;
+#pragma unroll
+              for (int i = 0; i < U / 2; ++i) {
+                if (i < half) {
+                  const float send = upper ? s[i] : s[i + half];
+                  const float keep = upper ? s[i + half] : s[i];
+                  s[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+                }
+              }
+              nv = half;
+            } else {
+              s[0] += __shfl_xor_sync(0xffffffffu, s[0], off);
+            }
+          }
+          {
+            const int span = LPR / U;  // lanes sharing one finished value
+            const int idx = sl / span;
+            const int k = (u0 + idx) * NSUB + sub;
+            if (sl % span == 0 && k < n_valid) a.out[base + k] = s[0];
           }
         }
       }

@@ -112,6 +112,24 @@ def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
     return out
 
 
+def csr_spmm_host(rowptr: torch.Tensor, colind: torch.Tensor, vals: torch.Tensor | None, B: torch.Tensor,
+                  nrows: int, ncols: int, out: torch.Tensor | None = None) -> torch.Tensor:
+    """C = A @ B from host (CPU) tensors to a host tensor, copies overlapped
+    with the kernels (pin the tensors for the overlap)."""
+    for name, t in (("rowptr", rowptr), ("colind", colind), ("B", B)):
+        if t.is_cuda or not t.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous host tensor")
+    if B.dtype not in _DT:
+        raise TypeError("B must be float32, bfloat16 or float16")
+    F = int(B.shape[1])
+    if out is None:
+        out = torch.empty((nrows, F), dtype=torch.float32, pin_memory=B.is_pinned())
+    dev = torch.device("cuda", torch.cuda.current_device())
+    _lib.call("gbs_csr_spmm_host", nrows, ncols, int(colind.numel()), _ptr(rowptr), _ptr(colind), _ptr(vals),
+              _ptr(B), _DT[B.dtype], F, _ptr(out), _stream(dev))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # B2SR
 # ---------------------------------------------------------------------------

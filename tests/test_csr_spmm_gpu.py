@@ -180,3 +180,31 @@ def test_column_blocks(cuda, dtype, cb):
     # so both are checked against FP64, not bitwise against each other.
     check_f32(g, B.float(), part)
     check_f32(g, B.float(), full)
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("dtype, vals", [(torch.float32, True), (torch.bfloat16, True), (torch.float32, False)])
+def test_host_buffer_pipelined(cuda, pinned, dtype, vals):
+    """gbs_csr_spmm_host (host A/B in, host C out, copies overlapped in row
+    ranges) against the FP64 oracle."""
+    g = G.flickr_like()
+    B32 = G.normal(21, 4, (g.ncols, 128))
+    Bh = B32.to(dtype)
+    args = [g.rowptr, g.colind, g.vals if vals else None, Bh]
+    if pinned:
+        args = [a.pin_memory() if a is not None else None for a in args]
+    C = ops.csr_spmm_host(*args, g.nrows, g.ncols)
+    assert not C.is_cuda
+    check_f32(g, Bh.float(), C, vals=vals)
+
+
+def test_workspace_reused_across_shapes(cuda):
+    """One workspace serving different shapes (different warp counts and
+    slot widths) in sequence: each result still matches FP64."""
+    ws = ops.SpmmWorkspace()
+    big = G.flickr_like()
+    small = small_graph(300, 257, 0.05, 3)
+    for g, F in ((big, 256), (small, 64), (big, 32), (small, 256), (big, 128)):
+        B = G.normal(F, 9, (g.ncols, F))
+        C = ops.csr_spmm(dev_csr(g, cuda), B.to(cuda), workspace=ws)
+        check_f32(g, B, C)
