@@ -266,11 +266,17 @@ GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t 
  * aligned.
  * ------------------------------------------------------------------------ */
 /* C (M x N int32, row-major): mode 0 = sum popc(a ^ b), 1 = sum popc(a & b),
- * 2 = 32*Kw - 2*xor (the +-1 dot product).  algo 0 = default (the faster
- * on GB300: CUDA-core __popc), 1 = CUDA-core __popc, 2 = tensor-core
- * mma.sync .b1 AND-popc (XOR from row popcounts). */
+ * 2 = 32*Kw - 2*xor (the +-1 dot product).  algo 0 = default (= 3, the
+ * fastest on GB300), 1 = CUDA-core __popc, 2 = tensor-core mma.sync .b1
+ * AND-popc (XOR from row popcounts), 3 = tcgen05 tensor cores on the bits
+ * expanded to FP8 {0, 1} (exact; allocates (M+N)*K bytes of temporaries,
+ * stream-ordered).  8192^3 XOR on GB300: 0.87 / 3.59 / 7.51 ms for 3 / 1 / 2. */
 GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
                       int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
+/* Number of bounded mbarrier waits that ran out in algo-3 launches of this
+ * process (0 in normal operation; each timeout also skips that tile's
+ * stores).  Synchronises with the device. */
+GBS_API gbs_status gbs_bmm_tc_timeouts(int *count);
 /* Drop-in for BMM32_Arow_Brow<float> (mm.cu:17-53) and BMM32_MT_M_S
  * (:59-75): C[r*B_width + c] = 32*A_width - 2*xor as float. */
 GBS_API gbs_status gbs_bmm32_arow_brow(const uint32_t *d_A, const uint32_t *d_B, float *d_C,

@@ -68,6 +68,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_pack_sign_rows": (st, [p, i32, i32, p, p]),
     "gbs_pack_sign_colud": (st, [p, i32, i32, p, p]),
     "gbs_bmm_b1": (st, [p, p, i32, i32, i32, i32, i32, p, p]),
+    "gbs_bmm_tc_timeouts": (st, [pi32]),
     "gbs_bmm32_arow_brow": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm32_bin": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm32s_bin": (st, [p, p, p, i32, i32, i32, p]),

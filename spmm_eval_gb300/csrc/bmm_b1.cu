@@ -13,8 +13,9 @@
 //   * popc : CUDA cores, each thread 8 x 8 outputs, XOR + POPC + ADD.
 //   * mma  : tensor cores, mma.sync.aligned.m16n8k256 .b1 AND-popc; XOR is
 //            recovered as popc(a) + popc(b) - 2 * and from row popcounts.
-// popc is the default: on GB300 it runs 8192^3 in 3.6 ms against 7.5 ms for
-// the .b1 tensor-core path.
+// Of these two, popc is the faster on GB300 (8192^3: 3.6 ms against 7.5 ms
+// for the .b1 tensor path); the default is the tcgen05 kernel in bmm_tc.cu
+// (0.87 ms), which multiplies the bits expanded to FP8.
 // Bit order inside a word does not matter to either (popcount of matching
 // K positions), so the reference layout is consumed as is.
 #include <cstdint>
@@ -247,8 +248,13 @@ __global__ void k_sign_words(const int32_t *__restrict__ X, int m, int k, int nb
   }
 }
 
+gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
+                      int ldc, cudaStream_t s);
+gbs_status bmm_tc_error_count(int *out);
+
 gbs_status bmm_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int algo,
                    int32_t *C, float *Cf, int ldc, cudaStream_t s) {
+  if (algo == 0 || algo == 3) return bmm_tc_run(A, B, M, N, Kw, mode, C, Cf, ldc, s);
   GBS_REQUIRE(M % 4 == 0 && N % 4 == 0, "bmm: M and N must be multiples of 4");
   GBS_REQUIRE((reinterpret_cast<uintptr_t>(A) & 15u) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0,
               "bmm: A and B must be 16-byte aligned");
@@ -285,18 +291,25 @@ gbs_status bmm_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, i
 
 using namespace gbs;
 
-// algo: 0 = default (the faster one measured on GB300: popc), 1 = popc CUDA cores,
-// 2 = tensor-core mma .b1.  8192^3 on GB300: popc 3.61 ms (304 TOPS), mma .b1
-// 7.55 ms (146 TOPS) -- the legacy binary tensor path is the slower one.
+// algo: 0 = default (the fastest measured on GB300: tcgen05 on FP8 {0,1}),
+// 1 = popc CUDA cores, 2 = tensor-core mma.sync .b1, 3 = tcgen05.  8192^3 XOR
+// counts on GB300: tcgen05 0.87 ms (1.26 P bit-ops/s, incl. the bit
+// expansion), popc 3.59 ms (306 T), mma.sync .b1 7.51 ms (146 T).
 extern "C" gbs_status gbs_bmm_b1(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode,
                                  int algo, int32_t *C, gbs_stream_t stream) {
   clear_error();
   GBS_REQUIRE(M >= 0 && N >= 0 && Kw >= 1, "bmm: bad sizes");
   GBS_REQUIRE(mode >= 0 && mode <= 2, "bmm: mode must be 0 (xor), 1 (and) or 2 (32*Kw - 2*xor)");
-  GBS_REQUIRE(algo >= 0 && algo <= 2, "bmm: algo must be 0, 1 or 2");
+  GBS_REQUIRE(algo >= 0 && algo <= 3, "bmm: algo must be 0, 1, 2 or 3");
   if (M == 0 || N == 0) return GBS_OK;
   GBS_REQUIRE(A && B && C, "bmm: null pointer");
   return bmm_run(A, B, M, N, Kw, mode, algo, C, nullptr, N, (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_bmm_tc_timeouts(int *count) {
+  clear_error();
+  GBS_REQUIRE(count != nullptr, "bmm tc timeouts: null output");
+  return bmm_tc_error_count(count);
 }
 
 extern "C" gbs_status gbs_bmm32_arow_brow(const uint32_t *A, const uint32_t *B, float *C, int A_height,
@@ -305,7 +318,7 @@ extern "C" gbs_status gbs_bmm32_arow_brow(const uint32_t *A, const uint32_t *B, 
   GBS_REQUIRE(A_height >= 0 && B_width >= 0 && A_width >= 1, "bmm32_arow_brow: bad sizes");
   if (A_height == 0 || B_width == 0) return GBS_OK;
   GBS_REQUIRE(A && B && C, "bmm32_arow_brow: null pointer");
-  return bmm_run(A, B, A_height, B_width, A_width, MODE_SIGNED, 1, nullptr, C, B_width,
+  return bmm_run(A, B, A_height, B_width, A_width, MODE_SIGNED, 0, nullptr, C, B_width,
                  (cudaStream_t)stream);
 }
 
@@ -318,7 +331,7 @@ static gbs_status bin_common(const uint32_t *A, const uint32_t *B, uint32_t *C, 
   const int Kw = (n + 31) / 32;
   DevBuf X;
   GBS_TRY(X.alloc(sizeof(int32_t) * (size_t)m * k, s));
-  GBS_TRY(bmm_run(A, B, m, k, Kw, MODE_XOR, 1, X.as<int32_t>(), nullptr, k, s));
+  GBS_TRY(bmm_run(A, B, m, k, Kw, MODE_XOR, 0, X.as<int32_t>(), nullptr, k, s));
   const long long warps = (long long)m * (k / 32);
   k_sign_words<<<(int)((warps * 32 + 255) / 256), 256, 0, s>>>(X.as<int32_t>(), m, k, n, layout, C);
   return check_launch("k_sign_words");

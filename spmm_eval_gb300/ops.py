@@ -257,7 +257,13 @@ def b2sr_aligned(Ab: B2SR):
 # Dense binary matmul (word-major operands, ToBit32ColUd layout)
 # ---------------------------------------------------------------------------
 BMM_XOR, BMM_AND, BMM_SIGNED = 0, 1, 2
-BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA = 0, 1, 2
+BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA, BMM_ALGO_TC = 0, 1, 2, 3
+
+
+def bmm_tc_timeouts() -> int:
+    n = C.c_int(0)
+    _lib.call("gbs_bmm_tc_timeouts", C.byref(n))
+    return int(n.value)
 
 
 def bmm_b1(A: torch.Tensor, B: torch.Tensor, mode: int = BMM_XOR, algo: int = BMM_ALGO_DEFAULT,

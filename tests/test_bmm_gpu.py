@@ -81,3 +81,13 @@ def test_sign_packed_dense_operands(cuda):
     got = ops.bmm_b1(pa, pb, ops.BMM_SIGNED).cpu().numpy()
     sa, sb = np.where(Xa >= 0, 1, -1), np.where(Xb >= 0, 1, -1)
     assert np.array_equal(got, sa @ sb.T)
+
+
+def test_default_algo_matches_popc(cuda):
+    rng = np.random.default_rng(17)
+    M, N, Kw = 256, 320, 12
+    A, B = words(rng, Kw, M), words(rng, Kw, N)
+    dA = torch.from_numpy(A.view(np.int32)).to(cuda)
+    dB = torch.from_numpy(B.view(np.int32)).to(cuda)
+    for mode in (ops.BMM_XOR, ops.BMM_AND, ops.BMM_SIGNED):
+        assert torch.equal(ops.bmm_b1(dA, dB, mode, ops.BMM_ALGO_DEFAULT), ops.bmm_b1(dA, dB, mode, ops.BMM_ALGO_POPC))
