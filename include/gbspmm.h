@@ -115,6 +115,27 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
                            float *d_C, void *d_workspace, size_t workspace_bytes,
                            gbs_stream_t stream);
 
+/* Column-partitioned plan.  When B is larger than L2, splitting A by column
+ * ranges into `parts` pieces (0 = choose: B bytes / (L2 / 2), a power of
+ * two <= 8, or 1 when B fits in L2 or rows of B are reused fewer than 8
+ * times) and accumulating one merge-path pass per piece keeps each pass's
+ * row gathers in L2 (FP32, 232,965 x 256 B on GB300: 8.0 ms -> 6.6 ms as 4
+ * parts).  The plan copies A's pattern and values into the parts (values
+ * captured at creation; rebuild after changing them); with one part it only
+ * records the caller's arrays, which must outlive it.  Synchronises the
+ * stream.  Workspace as gbs_csr_spmm_workspace_size(nrows, nnz, F, btype). */
+typedef struct gbs_csr_spmm_plan gbs_csr_spmm_plan;
+GBS_API gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz,
+                                    const int *d_rowptr, const int *d_colind,
+                                    const float *d_vals, gbs_dtype btype, int F,
+                                    int parts, gbs_stream_t stream,
+                                    gbs_csr_spmm_plan **out);
+GBS_API gbs_status gbs_csr_spmm_plan_parts(const gbs_csr_spmm_plan *plan, int *parts);
+GBS_API gbs_status gbs_csr_spmm_planned(const gbs_csr_spmm_plan *plan, const void *d_B,
+                                float *d_C, void *d_workspace,
+                                size_t workspace_bytes, gbs_stream_t stream);
+GBS_API gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *plan);
+
 /* Host-buffer form for callers that hold A, B and C in host memory, as the
  * reference's evalCSRSpmmFloatCuSPARSE does (test_spmm_full.cu:212-342):
  * copies in, C = A * B, copies out, and returns when h_C is filled.  A is

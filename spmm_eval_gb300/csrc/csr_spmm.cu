@@ -43,6 +43,7 @@ struct MergeArgs {
   int ldp;
   int P;
   long long D;
+  int accumulate;  // 1: C += A B (C read, added, written); 0: C = A B
 };
 
 template <int DT, int VEC, int LPR, int CH, int U>
@@ -132,6 +133,22 @@ struct MergeKernel {
     }
   }
 
+  // C row += acc (accumulating launches of a column-partitioned product).
+  static __device__ __forceinline__ void add_row(const MergeArgs &a, float *dst, int lane,
+                                                 float (&acc)[CH][VEC]) {
+    if (lane >= LPR) return;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + lane;
+      if (chunk >= a.nvec) continue;
+      float old[VEC];
+      load_vec_cg<VEC>(dst + (size_t)chunk * VEC, old);
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[c][q] = old[q] + acc[c][q];
+      store_vec<VEC, true>(dst + (size_t)chunk * VEC, acc[c]);
+    }
+  }
+
   // Called by every warp holding a piece of a split row r after it has
   // written that piece to its head or tail slot.  The last of the (w2 - w1 + 1) contributors sums the
   // pieces in warp order and writes C.
@@ -162,7 +179,13 @@ struct MergeKernel {
         load_vec_cg<VEC>(a.partials + (size_t)(2 * w2) * a.ldp + (size_t)chunk * VEC, x);
 #pragma unroll
         for (int q = 0; q < VEC; ++q) sum[q] += x[q];
-        store_vec<VEC, true>(a.C + (size_t)r * a.ldc + (size_t)chunk * VEC, sum);
+        float *dst = a.C + (size_t)r * a.ldc + (size_t)chunk * VEC;
+        if (a.accumulate) {
+          load_vec_cg<VEC>(dst, x);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) sum[q] = x[q] + sum[q];
+        }
+        store_vec<VEC, true>(dst, sum);
       }
     }
     if (lane == 0) a.counters[w1] = 0;
@@ -186,7 +209,8 @@ struct MergeKernel {
       const int rb = __ldg(a.rowptr + r) - a.rp_base, re = __ldg(a.rowptr + r + 1) - a.rp_base;
       accumulate(a, j, re, lane, acc);
       if (j == rb) {
-        write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
+        if (a.accumulate) add_row(a, a.C + (size_t)r * a.ldc, lane, acc);
+        else write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
       } else {  // head piece: the row started in an earlier warp
         write_row<false>(a, a.partials + (size_t)(2 * warp) * a.ldp, lane, acc);
         finish_split(a, r, lane);
@@ -333,9 +357,11 @@ gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col
 
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
-                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base) {
+                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base,
+                       int accumulate) {
   MergeArgs a;
   a.rp_base = rp_base;
+  a.accumulate = accumulate;
   a.nrows = nrows;
   a.nnz = nnz;
   a.F = Fw;
@@ -409,11 +435,11 @@ gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes
 
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream, int rp_base) {
+                    cudaStream_t stream, int rp_base, int accumulate) {
   for (int b = 0; b < p.nblk; ++b) {
     const char *Bb = reinterpret_cast<const char *>(B) + (size_t)b * p.Fw * p.esize;
     GBS_TRY(spmm_launch(p.v, p.P, nrows, nnz, rowptr, colind, vals, Bb, F, p.Fw,
-                        C + (size_t)b * p.Fw, F, ws, stream, rp_base));
+                        C + (size_t)b * p.Fw, F, ws, stream, rp_base, accumulate));
   }
   return GBS_OK;
 }

@@ -32,9 +32,10 @@ gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B
                      int col_block, SpmmPlan *p);
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
-                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base = 0);
+                       float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base = 0,
+                       int accumulate = 0);
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream, int rp_base = 0);
+                    cudaStream_t stream, int rp_base = 0, int accumulate = 0);
 
 }  // namespace gbs

@@ -112,6 +112,43 @@ def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
     return out
 
 
+class SpmmPlan:
+    """Column-partitioned SpMM plan for a fixed A, feature width and type
+    (parts = 0 lets the library choose from B's size against L2)."""
+
+    def __init__(self, A: CSR, F: int, dtype: torch.dtype = torch.float32, parts: int = 0):
+        A.validate_layout()
+        self.A, self.F, self.dtype = A, F, dtype
+        h = C.c_void_p()
+        _lib.call("gbs_csr_spmm_plan_create", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
+                  _ptr(A.vals), _DT[dtype], F, parts, _stream(A.rowptr.device), C.byref(h))
+        self._h = h
+        k = C.c_int(0)
+        _lib.call("gbs_csr_spmm_plan_parts", h, C.byref(k))
+        self.parts = int(k.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbs_csr_spmm_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self, B: torch.Tensor, out: torch.Tensor | None = None,
+            workspace: SpmmWorkspace | None = None) -> torch.Tensor:
+        _check_cuda("B", B, self.dtype)
+        if tuple(B.shape) != (self.A.ncols, self.F):
+            raise ValueError("B does not match the plan")
+        if out is None:
+            out = torch.empty((self.A.nrows, self.F), dtype=torch.float32, device=B.device)
+        ws = workspace or SpmmWorkspace()
+        buf = ws.get(spmm_workspace_bytes(self.A.nrows, self.A.nnz, self.F, self.dtype), B.device)
+        _lib.call("gbs_csr_spmm_planned", self._h, _ptr(B), _ptr(out), _ptr(buf), buf.numel(), _stream(B.device))
+        return out
+
+
 def csr_spmm_host(rowptr: torch.Tensor, colind: torch.Tensor, vals: torch.Tensor | None, B: torch.Tensor,
                   nrows: int, ncols: int, out: torch.Tensor | None = None) -> torch.Tensor:
     """C = A @ B from host (CPU) tensors to a host tensor, copies overlapped
