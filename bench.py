@@ -363,8 +363,10 @@ def run_ours(args):
     h_B = B_cpu.pin_memory()
     h_C = torch.empty((n, F), dtype=torch.float32).pin_memory()
 
+    hctx = ops.HostSpmmContext()
+
     def e2e_step():
-        ops.csr_spmm_host(h_rowptr, h_colind, h_vals, h_B, n, n, out=h_C)
+        ops.csr_spmm_host(h_rowptr, h_colind, h_vals, h_B, n, n, out=h_C, ctx=hctx)
 
     for _ in range(2):
         e2e_step()
@@ -422,12 +424,13 @@ def run_ours(args):
 def run_profile_case(args):
     """Short fixed launch sequences for ncu (2 warm-up launches, then
     `--steps` launches of each kernel, nothing else heavy):
-      full   : bench graph, FP32 then BF16 merge-path SpMM, F = 256
+      full   : bench graph, FP32 then BF16 planned merge-path SpMM, F = 256
+               (FP32: 4 column parts = 4 launches per step)
       eighth : same nodes (B still larger than L2), 1/8 of the degree
       fwdbwd : eighth graph, SpMM + A^T SpMM + SDDMM (FP32, then BF16)
       b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
                B2SR BMM F = 256
-      bmm    : 4096^3 binary GEMM, popc then mma .b1 (XOR counts)"""
+      bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 (XOR counts)"""
     import torch
     from spmm_eval_gb300 import graphs as G
     from spmm_eval_gb300 import ops
@@ -461,11 +464,14 @@ def run_profile_case(args):
                     T.spmm(tv, Gx, out=dH, workspace=ws)
                     ops.sddmm(Ap, Gx, Hx, out=dv)
         else:
+            plans = {torch.float32: ops.SpmmPlan(A, 256, torch.float32),
+                     torch.bfloat16: ops.SpmmPlan(A, 256, torch.bfloat16)}
             torch.cuda.synchronize()
             torch.cuda.empty_cache()
             for Bx in (B, Bh):
                 for _ in range(2 + args.steps):
-                    ops.csr_spmm(A, Bx, out=C, workspace=ws)
+                    plans[Bx.dtype].run(Bx, out=C, workspace=ws)
+            out["parts"] = {"f32": plans[torch.float32].parts, "bf16": plans[torch.bfloat16].parts}
         out.update(nodes=g.nrows, nnz=g.nnz)
     elif case == "b2sr":
         g = G.flickr_like(device=dev)
@@ -486,7 +492,7 @@ def run_profile_case(args):
         Aw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Bw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Co = torch.empty((M, M), dtype=torch.int32, device=dev)
-        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA):
+        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA, ops.BMM_ALGO_TC):
             for _ in range(2 + args.steps):
                 ops.bmm_b1(Aw, Bw, ops.BMM_XOR, algo, out=Co)
     torch.cuda.synchronize()

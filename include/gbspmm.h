@@ -141,10 +141,16 @@ GBS_API gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *plan);
  * copies in, C = A * B, copies out, and returns when h_C is filled.  A is
  * sent in row ranges of ~nnz/8 nonzeros so the copies overlap the kernels
  * (pinned host buffers are needed for the overlap; pageable ones work,
- * serialised).  Allocates its device buffers stream-ordered on `stream`. */
-GBS_API gbs_status gbs_csr_spmm_host(int nrows, int ncols, int nnz, const int *h_rowptr,
-                             const int *h_colind, const float *h_vals, const void *h_B,
-                             gbs_dtype btype, int F, float *h_C, gbs_stream_t stream);
+ * serialised).  ctx (optional) keeps device buffers, streams and events
+ * between calls; with ctx == NULL each call allocates its buffers
+ * stream-ordered on `stream`.  A context serves one call at a time. */
+typedef struct gbs_spmm_host_ctx gbs_spmm_host_ctx;
+GBS_API gbs_status gbs_spmm_host_ctx_create(gbs_spmm_host_ctx **out);
+GBS_API gbs_status gbs_spmm_host_ctx_destroy(gbs_spmm_host_ctx *ctx);
+GBS_API gbs_status gbs_csr_spmm_host(gbs_spmm_host_ctx *ctx, int nrows, int ncols, int nnz,
+                             const int *h_rowptr, const int *h_colind,
+                             const float *h_vals, const void *h_B, gbs_dtype btype,
+                             int F, float *h_C, gbs_stream_t stream);
 
 /* One-call FP32 form with the argument meaning of the cuSPARSE generic
  * SpMM used by the reference (alpha = 1, beta = 0, FP32 everywhere).

@@ -48,7 +48,9 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_cb": (st, [i32, i32, i32, p, p, p, p, i32, i32, i32, p, p, sz, p]),
     "gbs_csr_spmm_f32": (st, [i32, i32, i32, p, p, p, p, i32, p, p]),
-    "gbs_csr_spmm_host": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
+    "gbs_spmm_host_ctx_create": (st, [C.POINTER(p)]),
+    "gbs_spmm_host_ctx_destroy": (st, [p]),
+    "gbs_csr_spmm_host": (st, [p, i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr_spmm_plan_create": (st, [i32, i32, i32, p, p, p, i32, i32, i32, p, C.POINTER(p)]),
     "gbs_csr_spmm_plan_parts": (st, [p, pi32]),
     "gbs_csr_spmm_planned": (st, [p, p, p, p, sz, p]),

@@ -149,8 +149,27 @@ class SpmmPlan:
         return out
 
 
+class HostSpmmContext:
+    """Device buffers, streams and events kept between csr_spmm_host calls."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _lib.call("gbs_spmm_host_ctx_create", C.byref(h))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbs_spmm_host_ctx_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
 def csr_spmm_host(rowptr: torch.Tensor, colind: torch.Tensor, vals: torch.Tensor | None, B: torch.Tensor,
-                  nrows: int, ncols: int, out: torch.Tensor | None = None) -> torch.Tensor:
+                  nrows: int, ncols: int, out: torch.Tensor | None = None,
+                  ctx: HostSpmmContext | None = None) -> torch.Tensor:
     """C = A @ B from host (CPU) tensors to a host tensor, copies overlapped
     with the kernels (pin the tensors for the overlap)."""
     for name, t in (("rowptr", rowptr), ("colind", colind), ("B", B)):
@@ -162,8 +181,8 @@ def csr_spmm_host(rowptr: torch.Tensor, colind: torch.Tensor, vals: torch.Tensor
     if out is None:
         out = torch.empty((nrows, F), dtype=torch.float32, pin_memory=B.is_pinned())
     dev = torch.device("cuda", torch.cuda.current_device())
-    _lib.call("gbs_csr_spmm_host", nrows, ncols, int(colind.numel()), _ptr(rowptr), _ptr(colind), _ptr(vals),
-              _ptr(B), _DT[B.dtype], F, _ptr(out), _stream(dev))
+    _lib.call("gbs_csr_spmm_host", ctx._h if ctx is not None else None, nrows, ncols, int(colind.numel()),
+              _ptr(rowptr), _ptr(colind), _ptr(vals), _ptr(B), _DT[B.dtype], F, _ptr(out), _stream(dev))
     return out
 
 

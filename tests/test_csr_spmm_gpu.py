@@ -196,6 +196,10 @@ def test_host_buffer_pipelined(cuda, pinned, dtype, vals):
     C = ops.csr_spmm_host(*args, g.nrows, g.ncols)
     assert not C.is_cuda
     check_f32(g, Bh.float(), C, vals=vals)
+    ctx = ops.HostSpmmContext()
+    for _ in range(2):  # buffers kept in the context
+        C2 = ops.csr_spmm_host(*args, g.nrows, g.ncols, ctx=ctx)
+        check_f32(g, Bh.float(), C2, vals=vals)
 
 
 def test_workspace_reused_across_shapes(cuda):
