@@ -193,6 +193,15 @@ GBS_API gbs_status gbs_csr_spmm_transposed(const gbs_csr_transpose *T,
                                    gbs_dtype dtype, int F, float *d_dB,
                                    void *d_workspace, size_t workspace_bytes,
                                    gbs_stream_t stream);
+/* Fused backward of C = A H: dB = A^T dC (as gbs_csr_spmm_transposed) and
+ * dvals[e] = <dC[row(e)], H[col(e)]> (as gbs_sddmm, in A's entry order) in
+ * one pass over A^T's pattern, gathering each row of dC once for both.  dC,
+ * H: same dtype, 16-byte aligned, F a multiple of 4 (FP32) or 8 (16-bit).
+ * Workspace as gbs_csr_spmm_workspace_size(ncols, nnz, F, dtype). */
+GBS_API gbs_status gbs_spmm_backward(const gbs_csr_transpose *T, const float *d_t_vals,
+                             const void *d_dC, const void *d_H, gbs_dtype dtype,
+                             int F, float *d_dB, float *d_dvals, void *d_workspace,
+                             size_t workspace_bytes, gbs_stream_t stream);
 /* out[e] = sum_k G[row(e)][k] * H[col(e)][k], FP32 accumulation; G nrows x F
  * and H ncols x F in dtype. */
 GBS_API gbs_status gbs_sddmm(int nrows, int ncols, int nnz, const int *d_rowptr,

@@ -1,0 +1,104 @@
+// Fused backward of C = A H in one pass over A^T's pattern:
+//   dH[c]     = sum_r A[r][c] dC[r]          (merge-path SpMM on A^T)
+//   dvals[e]  = <dC[r], H[c]>  for e = (r, c) (SDDMM on A's pattern)
+// A warp walking row c of A^T gathers dC[r] for every entry (r, c) for the
+// SpMM anyway; with H[c] held in registers the SDDMM dot product costs only
+// FMAs and a butterfly reduction, and the separate SDDMM pass -- a second
+// gather of every row -- disappears.  dvals is written in A's entry order
+// through the transpose's permutation.
+#include "common.cuh"
+#include "csr_spmm.cuh"
+#include "merge_kernel.cuh"
+#include "transpose.cuh"
+
+namespace gbs {
+
+template <int DT, int VEC, int LPR, int CH, int U, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_csr_spmm_bwd(MergeArgs a) {
+  MergeKernel<DT, VEC, LPR, CH, U, true>::run(a);
+}
+
+namespace {
+
+template <int DT, int VEC, int LPR, int CH>
+SpmmVariant mkb() {
+  constexpr int UCAP = CH == 1 ? 4 : (CH == 2 ? 2 : 1);
+  constexpr int U = UCAP < LPR ? UCAP : LPR;
+  // accumulators + blocked partials + H row + loads in flight
+  constexpr int EST = 24 + 3 * CH * VEC + U * CH * 4 + 2 * U;
+  constexpr int MINB = EST <= 64 ? 4 : (EST <= 80 ? 3 : (EST <= 128 ? 2 : 1));
+  return SpmmVariant{(const void *)&k_csr_spmm_bwd<DT, VEC, LPR, CH, U, MINB>, VEC, LPR, CH};
+}
+
+template <int DT, int VEC>
+bool pickb(int nvec, SpmmVariant *v) {
+  if (nvec <= 1) { *v = mkb<DT, VEC, 1, 1>(); return true; }
+  if (nvec <= 2) { *v = mkb<DT, VEC, 2, 1>(); return true; }
+  if (nvec <= 4) { *v = mkb<DT, VEC, 4, 1>(); return true; }
+  if (nvec <= 8) { *v = mkb<DT, VEC, 8, 1>(); return true; }
+  if (nvec <= 16) { *v = mkb<DT, VEC, 16, 1>(); return true; }
+  if (nvec <= 32) { *v = mkb<DT, VEC, 32, 1>(); return true; }
+  if (nvec <= 64) { *v = mkb<DT, VEC, 32, 2>(); return true; }
+  if (nvec <= 128) { *v = mkb<DT, VEC, 32, 4>(); return true; }
+  if (nvec <= 256) { *v = mkb<DT, VEC, 32, 8>(); return true; }
+  return false;
+}
+
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" gbs_status gbs_spmm_backward(const gbs_csr_transpose *T, const float *t_vals, const void *dC,
+                                        const void *H, gbs_dtype dtype, int F, float *dB, float *dvals, void *ws,
+                                        size_t ws_bytes, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(T != nullptr, "spmm backward: null transpose handle");
+  GBS_REQUIRE(dtype == GBS_F32 || dtype == GBS_BF16 || dtype == GBS_F16, "spmm backward: bad dtype");
+  GBS_REQUIRE(F >= 1, "spmm backward: F must be >= 1");
+  const int n = T->ncols;  // rows of A^T
+  if (n == 0) return GBS_OK;
+  GBS_REQUIRE(dC && H && dB && dvals, "spmm backward: null pointer");
+  const int dt = dtype == GBS_F32 ? DT_F32 : (dtype == GBS_BF16 ? DT_BF16 : DT_F16);
+  const uintptr_t al = reinterpret_cast<uintptr_t>(dC) | reinterpret_cast<uintptr_t>(H) |
+                       reinterpret_cast<uintptr_t>(dB);
+  const int vec = dt == DT_F32 ? 4 : 8;
+  GBS_REQUIRE((al & 15u) == 0 && F % vec == 0,
+              "spmm backward: needs 16-byte aligned dC, H, dB and F a multiple of 4 (FP32) / 8 (16-bit)");
+  SpmmVariant v{};
+  bool ok = dt == DT_F32 ? pickb<DT_F32, 4>(F / 4, &v)
+                         : (dt == DT_BF16 ? pickb<DT_BF16, 8>(F / 8, &v) : pickb<DT_F16, 8>(F / 8, &v));
+  if (!ok) return fail(GBS_ERR_UNSUPPORTED, "spmm backward: F too large (FP32 <= 1024, 16-bit <= 2048)");
+  int P = 0;
+  GBS_TRY(spmm_warps(v, n, T->nnz, &P));
+  GBS_REQUIRE(ws != nullptr && ws_bytes >= spmm_workspace_bytes(P, F),
+              "spmm backward: workspace missing or too small (size it as gbs_csr_spmm_workspace_size(ncols, nnz, F))");
+  MergeArgs a;
+  a.nrows = n;
+  a.nnz = T->nnz;
+  a.F = F;
+  a.nvec = F / v.vec;
+  a.ldb = F;
+  a.ldc = F;
+  a.rowptr = T->t_rowptr;
+  a.rp_base = 0;
+  a.colind = T->t_colind;
+  a.vals = t_vals;
+  a.B = dC;
+  a.C = dB;
+  a.ldp = (int)align_up((size_t)F, 4);
+  a.P = P;
+  const long long total = (long long)n + T->nnz;
+  a.D = (total + P - 1) / P;
+  if (a.D < 1) a.D = 1;
+  a.counters = reinterpret_cast<int *>(ws);
+  a.partials = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + spmm_counter_bytes());
+  a.accumulate = 0;
+  a.H = H;
+  a.dvals = dvals;
+  a.perm = T->perm;
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3((unsigned)((P * 32 + 255) / 256)), dim3(256), args, 0,
+                                (cudaStream_t)stream));
+  return GBS_OK;
+}

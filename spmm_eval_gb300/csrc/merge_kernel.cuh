@@ -1,0 +1,292 @@
+// Merge-path CSR SpMM kernel template shared by the forward entry points
+// (csr_spmm.cu) and the fused backward (csr_spmm_bwd.cu).
+//
+// Schedule.  The merge of the row-end list rowptr[1..n] with the nonzero
+// indices 0..nnz-1 has n + nnz events; warp w owns events [w*D, (w+1)*D).
+// A row whose events all fall in one warp is summed by that warp in CSR
+// order and written to C directly.  A row cut by a share boundary is summed
+// piecewise: every warp holding a piece writes it to a workspace slot, bumps
+// a per-row arrival counter, and the warp that arrives last adds the pieces
+// in warp order and writes C (then resets the counter).  Nothing waits on
+// another warp, and the addition order depends only on (n, nnz, P), so the
+// result is bitwise reproducible for a given device and F.
+//
+// Lane mapping.  A feature row of F elements is nvec = F / VEC 16-byte
+// chunks.  LPR = min(32, pow2 >= nvec) lanes cover one row (CH chunks each);
+// the NSUB = 32 / LPR sub-groups of a warp take interleaved nonzeros of the
+// same row and are folded together with xor-shuffles at the row end.
+//
+// SD (fused SDDMM, backward only): the warp also keeps row r of H in
+// registers and, for every entry (r, c) it gathers, reduces <B[c], H[r]>
+// across the row's lanes and stores it at dvals[perm[e]] -- the value
+// gradient of A in C = A^T-pass order mapped back to A's order.
+#pragma once
+
+#include "common.cuh"
+#include "feat.cuh"
+#include "merge.cuh"
+
+namespace gbs {
+
+struct MergeArgs {
+  int nrows, nnz;
+  int F;     // width of the column block handled by this launch
+  int nvec;  // F / VEC
+  long long ldb, ldc;  // row strides of B and C (elements)
+  const int *rowptr;  // rowptr[0] == rp_base; colind/vals point at entry rp_base
+  int rp_base;
+  const int *colind;
+  const float *vals;  // may be null: binary A
+  const void *B;
+  float *C;
+  float *partials;  // [2P][ldp]
+  int *counters;    // [P]
+  int ldp;
+  int P;
+  long long D;
+  int accumulate;  // 1: C += A B (C read, added, written); 0: C = A B
+  // fused SDDMM (SD kernels only)
+  const void *H;     // rows indexed like C, F elements, B's type
+  float *dvals;      // output, indexed through perm
+  const int *perm;   // entry e of this matrix -> index in dvals
+};
+
+template <int DT, int VEC, int LPR, int CH, int U, bool SD = false>
+struct MergeKernel {
+  static constexpr int NSUB = 32 / LPR;
+  static constexpr int KPS = LPR;  // nonzeros per sub-group in a batch of 32
+  using F_ = Feat<DT, VEC>;
+  using raw = typename F_::raw;
+
+  // Sum nonzeros [jb, je) of one row into acc (this lane's columns, this
+  // lane's sub-group share).
+  static __device__ __forceinline__ void accumulate(const MergeArgs &a, int jb, int je,
+                                                    int lane, float (&acc)[CH][VEC],
+                                                    const float (&h)[CH][VEC]) {
+    const int sub = lane / LPR;
+    const int sl = lane % LPR;
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
+
+    for (int base = jb; base < je; base += 32) {
+      const int n_valid = min(32, je - base);
+      int my_col = 0;
+      float my_val = 0.f;
+      if (lane < n_valid) {
+        my_col = ld_stream_i32(a.colind + base + lane);
+        my_val = a.vals ? ld_stream_f32(a.vals + base + lane) : 1.f;
+      }
+      // blocked summation: each batch of 32 nonzeros is summed into a fresh
+      // partial that is then added to the row total (error ~ sqrt(32) +
+      // sqrt(deg/32) roundings instead of sqrt(deg))
+      float bs[CH][VEC];
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) bs[c][q] = 0.f;
+      // rounds of U nonzeros per sub-group; a runtime trip count (not an
+      // unrolled loop with early exits) keeps the loads of one round together
+      const int rounds = (n_valid + U * NSUB - 1) / (U * NSUB);
+#pragma unroll 1
+      for (int rd = 0; rd < rounds; ++rd) {
+        const int u0 = rd * U;
+        raw bv[U][CH];
+        float vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int k = ((u0 + u) * NSUB + sub) & 31;
+          const int col = __shfl_sync(0xffffffffu, my_col, k);
+          const float v = __shfl_sync(0xffffffffu, my_val, k);
+          const bool ok = (u0 + u) * NSUB + sub < n_valid;
+          vv[u] = ok ? v : 0.f;
+          const size_t rowbase = (size_t)col * (size_t)a.ldb;
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            const int chunk = c * LPR + sl;
+            if (ok && chunk < a.nvec) bv[u][c] = F_::load(a.B, rowbase + (size_t)chunk * VEC);
+            else bv[u][c] = F_::zero();
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
+        if constexpr (SD) sddmm_round(a, base, u0, n_valid, sub, sl, h, bv);
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) acc[c][q] += bs[c][q];
+    }
+    // fold the sub-groups (fixed tree order)
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1)
+#pragma unroll
+      for (int c = 0; c < CH; ++c)
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) acc[c][q] += __shfl_xor_sync(0xffffffffu, acc[c][q], off);
+  }
+
+  // Fused SDDMM for one round of U entries per sub-group: dot products of the
+  // gathered rows with the H row in registers, reduced over the LPR lanes by
+  // a multi-value butterfly ((U - 1) + log2(LPR / U) shuffles per U entries).
+  static __device__ __forceinline__ void sddmm_round(const MergeArgs &a, int base, int u0, int n_valid, int sub,
+                                                     int sl, const float (&h)[CH][VEC], const raw (&bv)[U][CH]) {
+    float s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      s[u] = 0.f;
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        float x[VEC];
+        F_::widen(x, bv[u][c]);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) s[u] = fmaf(h[c][q], x[q], s[u]);
+      }
+    }
+    int nv = U;
+#pragma unroll
+    for (int off = LPR / 2; off >= 1; off >>= 1) {
+      if (nv > 1) {
+        const int half = nv / 2;
+        const bool upper = (sl & off) != 0;
+#pragma unroll
+        for (int i = 0; i < U / 2; ++i) {
+          if (i < half) {
+            const float send = upper ? s[i] : s[i + half];
+            const float keep = upper ? s[i + half] : s[i];
+            s[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+          }
+        }
+        nv = half;
+      } else {
+        s[0] += __shfl_xor_sync(0xffffffffu, s[0], off);
+      }
+    }
+    const int span = LPR / U;
+    const int k = (u0 + sl / span) * NSUB + sub;
+    if (sl % span == 0 && k < n_valid) a.dvals[__ldg(a.perm + a.rp_base + base + k)] = s[0];
+  }
+
+  // H row r (this lane's chunks), widened to FP32.
+  static __device__ __forceinline__ void load_h(const MergeArgs &a, int r, int lane, float (&h)[CH][VEC]) {
+    const int sl = lane % LPR;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + sl;
+      if (SD && chunk < a.nvec) F_::widen(h[c], F_::load(a.H, (size_t)r * a.F + (size_t)chunk * VEC));
+      else
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) h[c][q] = 0.f;
+    }
+  }
+
+  template <bool STREAM>
+  static __device__ __forceinline__ void write_row(const MergeArgs &a, float *dst, int lane,
+                                                   const float (&acc)[CH][VEC]) {
+    if (lane >= LPR) return;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + lane;
+      if (chunk < a.nvec) store_vec<VEC, STREAM>(dst + (size_t)chunk * VEC, acc[c]);
+    }
+  }
+
+  // C row += acc (accumulating launches of a column-partitioned product).
+  static __device__ __forceinline__ void add_row(const MergeArgs &a, float *dst, int lane,
+                                                 float (&acc)[CH][VEC]) {
+    if (lane >= LPR) return;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int chunk = c * LPR + lane;
+      if (chunk >= a.nvec) continue;
+      float old[VEC];
+      load_vec_cg<VEC>(dst + (size_t)chunk * VEC, old);
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[c][q] = old[q] + acc[c][q];
+      store_vec<VEC, true>(dst + (size_t)chunk * VEC, acc[c]);
+    }
+  }
+
+  // Called by every warp holding a piece of a split row r after it has
+  // written that piece to its head or tail slot.  The last of the (w2 - w1 + 1) contributors sums the
+  // pieces in warp order and writes C.
+  static __device__ __forceinline__ void finish_split(const MergeArgs &a, int r, int lane) {
+    const int rb = __ldg(a.rowptr + r) - a.rp_base, re = __ldg(a.rowptr + r + 1) - a.rp_base;
+    const int w1 = (int)(((long long)rb + r) / a.D);
+    const int w2 = (int)(((long long)re + r) / a.D);
+    __threadfence();
+    __syncwarp();
+    int old = 0;
+    if (lane == 0) old = atomicAdd(a.counters + w1, 1);
+    old = __shfl_sync(0xffffffffu, old, 0);
+    if (old != w2 - w1) return;
+    __threadfence();
+    if (lane < LPR) {
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int chunk = c * LPR + lane;
+        if (chunk >= a.nvec) continue;
+        float sum[VEC], x[VEC];
+        // tail piece of w1, middle pieces (tail slots), head piece of w2
+        load_vec_cg<VEC>(a.partials + (size_t)(2 * w1 + 1) * a.ldp + (size_t)chunk * VEC, sum);
+        for (int w = w1 + 1; w < w2; ++w) {
+          load_vec_cg<VEC>(a.partials + (size_t)(2 * w + 1) * a.ldp + (size_t)chunk * VEC, x);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) sum[q] += x[q];
+        }
+        load_vec_cg<VEC>(a.partials + (size_t)(2 * w2) * a.ldp + (size_t)chunk * VEC, x);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) sum[q] += x[q];
+        float *dst = a.C + (size_t)r * a.ldc + (size_t)chunk * VEC;
+        if (a.accumulate) {
+          load_vec_cg<VEC>(dst, x);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) sum[q] = x[q] + sum[q];
+        }
+        store_vec<VEC, true>(dst, sum);
+      }
+    }
+    if (lane == 0) a.counters[w1] = 0;
+  }
+
+  static __device__ void run(const MergeArgs &a) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (warp >= a.P) return;
+    const long long total = (long long)a.nrows + a.nnz;
+    const long long d0 = min((long long)warp * a.D, total);
+    const long long d1 = min((long long)(warp + 1) * a.D, total);
+    if (d0 >= d1) return;
+    const int i0 = merge_search(a.rowptr, a.nrows, a.nnz, d0, a.rp_base);
+    const int i1 = merge_search(a.rowptr, a.nrows, a.nnz, d1, a.rp_base);
+    int j = (int)(d0 - i0);
+    const int j1 = (int)(d1 - i1);
+
+    float acc[CH][VEC];
+    float h[CH][VEC];
+    for (int r = i0; r < i1; ++r) {
+      const int rb = __ldg(a.rowptr + r) - a.rp_base, re = __ldg(a.rowptr + r + 1) - a.rp_base;
+      if constexpr (SD) load_h(a, r, lane, h);
+      accumulate(a, j, re, lane, acc, h);
+      if (j == rb) {
+        if (a.accumulate) add_row(a, a.C + (size_t)r * a.ldc, lane, acc);
+        else write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
+      } else {  // head piece: the row started in an earlier warp
+        write_row<false>(a, a.partials + (size_t)(2 * warp) * a.ldp, lane, acc);
+        finish_split(a, r, lane);
+      }
+      j = re;
+    }
+    if (j < j1) {  // tail (or middle) piece of row i1: continues past d1
+      if constexpr (SD) load_h(a, i1, lane, h);
+      accumulate(a, j, j1, lane, acc, h);
+      write_row<false>(a, a.partials + (size_t)(2 * warp + 1) * a.ldp, lane, acc);
+      finish_split(a, i1, lane);
+    }
+  }
+};
+
+}  // namespace gbs

@@ -11,13 +11,7 @@
 #include "csr_spmm.cuh"
 #include "util.cuh"
 
-struct gbs_csr_transpose {
-  int nrows, ncols, nnz;
-  int device;
-  int *t_rowptr;  // ncols + 1
-  int *t_colind;  // nnz
-  int *perm;      // nnz
-};
+#include "transpose.cuh"
 
 namespace gbs {
 

@@ -402,6 +402,24 @@ class CSRTranspose:
         return out
 
 
+def spmm_backward(T: "CSRTranspose", t_vals: torch.Tensor | None, dC: torch.Tensor, H: torch.Tensor,
+                  dB: torch.Tensor | None = None, dvals: torch.Tensor | None = None,
+                  workspace: SpmmWorkspace | None = None):
+    """Fused backward of C = A H: (dB = A^T dC, dvals[e] = <dC[row e], H[col e]>)."""
+    _check_cuda("dC", dC, tuple(_DT))
+    _check_cuda("H", H, dC.dtype)
+    F = int(dC.shape[1])
+    if dB is None:
+        dB = torch.empty((T.ncols, F), dtype=torch.float32, device=dC.device)
+    if dvals is None:
+        dvals = torch.empty(T.nnz, dtype=torch.float32, device=dC.device)
+    ws = workspace or SpmmWorkspace()
+    buf = ws.get(spmm_workspace_bytes(T.ncols, T.nnz, F, dC.dtype), dC.device)
+    _lib.call("gbs_spmm_backward", T._h, _ptr(t_vals), _ptr(dC), _ptr(H), _DT[dC.dtype], F, _ptr(dB),
+              _ptr(dvals), _ptr(buf), buf.numel(), _stream(dC.device))
+    return dB, dvals
+
+
 def sddmm(A: CSR, G: torch.Tensor, H: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """out[e] = <G[row(e)], H[col(e)]> on A's pattern (FP32)."""
     A.validate_layout()

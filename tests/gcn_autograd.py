@@ -1,8 +1,8 @@
 """Test-harness-only autograd wrapper of the library's SpMM forward and
 backward kernels (the library itself exposes them through the C ABI):
   forward : Y = A(vals) @ H            (merge-path CSR SpMM)
-  backward: dH = A^T @ dY              (cached transpose + same SpMM)
-            dvals[e] = <dY[row e], H[col e]>   (SDDMM on A's pattern)
+  backward: dH = A^T @ dY and dvals[e] = <dY[row e], H[col e]>, fused in
+            one pass over the cached transpose (gbs_spmm_backward)
 Features (H, dY) are handed to the kernels in `feat_dtype` (FP32 or BF16);
 accumulation and outputs are FP32."""
 import torch
@@ -25,9 +25,8 @@ class SpMMFunction(torch.autograd.Function):
         vals, Hk = ctx.saved_tensors
         p, T = ctx.pattern, ctx.transpose
         Gk = gY.detach().to(ctx.feat_dtype).contiguous()
-        dH = T.spmm(T.values(vals.detach().contiguous()), Gk)
-        A = ops.CSR(p.rowptr, p.colind, None, p.nrows, p.ncols)
-        dvals = ops.sddmm(A, Gk, Hk)
+        # fused: dH = A^T dY and dvals = SDDMM(dY, H) in one pass over A^T
+        dH, dvals = ops.spmm_backward(T, T.values(vals.detach().contiguous()), Gk, Hk)
         return dvals, dH, None, None, None
 
 

@@ -172,3 +172,26 @@ def test_gradcheck_fd_512_subgraph(cuda, feat_dtype, rtol):
             g_k = grad.reshape(-1)[idx].double()
             scale = grad.abs().max().double()
             assert abs(g_k - fd) <= rtol * scale + 1e-7, (name, idx, float(g_k), float(fd))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("F", [8, 32, 64, 256])
+def test_fused_backward_matches_separate(cuda, dtype, F):
+    """gbs_spmm_backward (A^T SpMM + SDDMM in one pass) against FP64 oracles
+    of both outputs."""
+    g = G.gcn_normalize(G.flickr_like())
+    n = g.nrows
+    Gm = G.normal(F, 21, (n, F))
+    Hm = G.normal(F, 22, (n, F))
+    Gd, Hd = Gm.to(dtype).to(cuda), Hm.to(dtype).to(cuda)
+    T = ops.CSRTranspose(dev(g, cuda, False))
+    tv = T.values(g.vals.to(cuda))
+    dB, dv = ops.spmm_backward(T, tv, Gd, Hd)
+    rp, ci, v = g.rowptr.numpy(), g.colind.numpy(), g.vals.numpy()
+    Gr, Hr = Gd.float().cpu().numpy(), Hd.float().cpu().numpy()
+    wrp, wci, wpm = oracle.csr_transpose(n, n, rp, ci)
+    ref, mag = oracle.csr_spmm_f64(wrp, wci, v[wpm], Gr)
+    assert oracle.rel_err(dB.cpu().numpy(), ref, mag)[0] <= 1e-5
+    refv = oracle.sddmm_f64(rp, ci, Gr, Hr)
+    S = sddmm_scale(rp, ci, Gr, Hr)
+    assert np.max(np.abs(dv.cpu().numpy() - refv) / np.maximum(S, 1e-30)) <= 1e-5
