@@ -11,6 +11,15 @@ enum { DT_F32 = 0, DT_BF16 = 1, DT_F16 = 2 };
 
 inline int dt_bytes(int dt) { return dt == DT_F32 ? 4 : 2; }
 
+// acc0 += v * x0, acc1 += v * x1 as one packed sm_100+ FFMA2 (each half
+// rounds exactly like fmaf).
+__device__ __forceinline__ void fma2(float &acc0, float &acc1, float v, float x0, float x1) {
+  asm("{\n .reg .b64 va, xa, ca;\n mov.b64 va, {%2, %2};\n mov.b64 xa, {%3, %4};\n"
+      " mov.b64 ca, {%0, %1};\n fma.rn.f32x2 ca, va, xa, ca;\n mov.b64 {%0, %1}, ca;\n}"
+      : "+f"(acc0), "+f"(acc1)
+      : "f"(v), "f"(x0), "f"(x1));
+}
+
 template <int DT, int VEC>
 struct Feat;
 
@@ -23,10 +32,8 @@ struct Feat<DT_F32, 4> {
   }
   static __device__ __forceinline__ raw zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
   static __device__ __forceinline__ void fma(float *acc, float v, const raw &r) {
-    acc[0] = fmaf(v, r.x, acc[0]);
-    acc[1] = fmaf(v, r.y, acc[1]);
-    acc[2] = fmaf(v, r.z, acc[2]);
-    acc[3] = fmaf(v, r.w, acc[3]);
+    fma2(acc[0], acc[1], v, r.x, r.y);
+    fma2(acc[2], acc[3], v, r.z, r.w);
   }
   static __device__ __forceinline__ void widen(float *out, const raw &r) {
     out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
@@ -56,14 +63,10 @@ struct Feat<DT_BF16, 8> {
   }
   static __device__ __forceinline__ raw zero() { return make_uint4(0, 0, 0, 0); }
   static __device__ __forceinline__ void fma(float *acc, float v, const raw &r) {
-    acc[0] = fmaf(v, bf16lo(r.x), acc[0]);
-    acc[1] = fmaf(v, bf16hi(r.x), acc[1]);
-    acc[2] = fmaf(v, bf16lo(r.y), acc[2]);
-    acc[3] = fmaf(v, bf16hi(r.y), acc[3]);
-    acc[4] = fmaf(v, bf16lo(r.z), acc[4]);
-    acc[5] = fmaf(v, bf16hi(r.z), acc[5]);
-    acc[6] = fmaf(v, bf16lo(r.w), acc[6]);
-    acc[7] = fmaf(v, bf16hi(r.w), acc[7]);
+    fma2(acc[0], acc[1], v, bf16lo(r.x), bf16hi(r.x));
+    fma2(acc[2], acc[3], v, bf16lo(r.y), bf16hi(r.y));
+    fma2(acc[4], acc[5], v, bf16lo(r.z), bf16hi(r.z));
+    fma2(acc[6], acc[7], v, bf16lo(r.w), bf16hi(r.w));
   }
   static __device__ __forceinline__ void widen(float *out, const raw &r) {
     out[0] = bf16lo(r.x); out[1] = bf16hi(r.x); out[2] = bf16lo(r.y); out[3] = bf16hi(r.y);
@@ -81,14 +84,10 @@ struct Feat<DT_F16, 8> {
   static __device__ __forceinline__ raw zero() { return make_uint4(0, 0, 0, 0); }
   static __device__ __forceinline__ void fma(float *acc, float v, const raw &r) {
     float2 a = h2f2(r.x), b = h2f2(r.y), c = h2f2(r.z), d = h2f2(r.w);
-    acc[0] = fmaf(v, a.x, acc[0]);
-    acc[1] = fmaf(v, a.y, acc[1]);
-    acc[2] = fmaf(v, b.x, acc[2]);
-    acc[3] = fmaf(v, b.y, acc[3]);
-    acc[4] = fmaf(v, c.x, acc[4]);
-    acc[5] = fmaf(v, c.y, acc[5]);
-    acc[6] = fmaf(v, d.x, acc[6]);
-    acc[7] = fmaf(v, d.y, acc[7]);
+    fma2(acc[0], acc[1], v, a.x, a.y);
+    fma2(acc[2], acc[3], v, b.x, b.y);
+    fma2(acc[4], acc[5], v, c.x, c.y);
+    fma2(acc[6], acc[7], v, d.x, d.y);
   }
   static __device__ __forceinline__ void widen(float *out, const raw &r) {
     float2 a = h2f2(r.x), b = h2f2(r.y), c = h2f2(r.z), d = h2f2(r.w);
