@@ -426,7 +426,8 @@ def run_profile_case(args):
       fwdbwd : eighth graph, SpMM + A^T SpMM + SDDMM (FP32, then BF16)
       b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
                B2SR BMM F = 256
-      bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 (XOR counts)"""
+      bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 per tile, tcgen05
+               persistent (XOR counts)"""
     import torch
     from spmm_eval_gb300 import graphs as G
     from spmm_eval_gb300 import ops
@@ -488,7 +489,7 @@ def run_profile_case(args):
         Aw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Bw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Co = torch.empty((M, M), dtype=torch.int32, device=dev)
-        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA, ops.BMM_ALGO_TC):
+        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA, ops.BMM_ALGO_TC, ops.BMM_ALGO_TC_PERSIST):
             for _ in range(2 + args.steps):
                 ops.bmm_b1(Aw, Bw, ops.BMM_XOR, algo, out=Co)
     torch.cuda.synchronize()

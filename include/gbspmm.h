@@ -52,6 +52,11 @@ typedef enum gbs_dtype { GBS_F32 = 0, GBS_BF16 = 1, GBS_F16 = 2 } gbs_dtype;
 GBS_API const char *gbs_last_error(void);
 /* ABI version of this header (bumped on incompatible change). */
 GBS_API int gbs_abi_version(void);
+/* Entry points that document temporary allocations take them from a
+ * library-owned stream-ordered pool on the current device, which keeps up to
+ * 8 GiB of freed temporaries mapped between calls.  This returns all of the
+ * pool's unused memory to the device.  No counterpart in the reference. */
+GBS_API gbs_status gbs_pool_trim(void);
 
 /* ------------------------------------------------------------------------
  * Matrix Market ingest (host).  Same result as readMtx<float>(...,
@@ -302,14 +307,17 @@ GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t 
  * aligned.
  * ------------------------------------------------------------------------ */
 /* C (M x N int32, row-major): mode 0 = sum popc(a ^ b), 1 = sum popc(a & b),
- * 2 = 32*Kw - 2*xor (the +-1 dot product).  algo 0 = default (= 3, the
+ * 2 = 32*Kw - 2*xor (the +-1 dot product).  algo 0 = default (= 4, the
  * fastest on GB300), 1 = CUDA-core __popc, 2 = tensor-core mma.sync .b1
  * AND-popc (XOR from row popcounts), 3 = tcgen05 tensor cores on the bits
- * expanded to FP8 {0, 1} (exact; allocates (M+N)*K bytes of temporaries,
- * stream-ordered).  8192^3 XOR on GB300: 0.87 / 3.59 / 7.51 ms for 3 / 1 / 2. */
+ * expanded to FP8 {0, 1}, one CTA per 128 x 256 tile, 4 = the same MMAs in
+ * a persistent warp-specialised kernel (one CTA per SM, two TMEM
+ * accumulators so a tile's epilogue overlaps the next tile's MMAs).  3 and 4
+ * are exact and allocate (M+N)*K bytes of temporaries, stream-ordered.
+ * 8192^3 XOR on GB300: 0.87 / 3.59 / 7.51 ms for 3 / 1 / 2. */
 GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
                       int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
-/* Number of bounded mbarrier waits that ran out in algo-3 launches of this
+/* Number of bounded mbarrier waits that ran out in algo-3/4 launches of this
  * process (0 in normal operation; each timeout also skips that tile's
  * stores).  Synchronises with the device. */
 GBS_API gbs_status gbs_bmm_tc_timeouts(int *count);

@@ -41,6 +41,7 @@ class HostCSR(C.Structure):
 SIGNATURES: dict[str, tuple] = {
     "gbs_last_error": (C.c_char_p, []),
     "gbs_abi_version": (C.c_int, []),
+    "gbs_pool_trim": (st, []),
     "gbs_mtx_read": (st, [C.c_char_p, C.POINTER(HostCSR)]),
     "gbs_host_csr_free": (None, [C.POINTER(HostCSR)]),
     "gbs_csr_spmm_workspace_size": (st, [i32, i32, i32, i32, psz]),

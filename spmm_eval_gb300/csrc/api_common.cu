@@ -3,6 +3,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "util.cuh"
 
 namespace gbs {
 
@@ -37,7 +38,41 @@ gbs_status device_info(DeviceInfo *out) {
   return GBS_OK;
 }
 
+gbs_status lib_pool(cudaMemPool_t *out) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "device ordinal >= 64");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p;
+    GBS_CUDA_TRY(cudaMemPoolCreate(&p, &props));
+    unsigned long long keep = kPoolKeepBytes;
+    cudaError_t e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(p);
+      return cuda_fail(e, "cudaMemPoolSetAttribute");
+    }
+    pools[dev] = p;
+  }
+  *out = pools[dev];
+  return GBS_OK;
+}
+
 }  // namespace gbs
+
+extern "C" gbs_status gbs_pool_trim(void) {
+  gbs::clear_error();
+  cudaMemPool_t p;
+  GBS_TRY(gbs::lib_pool(&p));
+  GBS_CUDA_TRY(cudaMemPoolTrimTo(p, 0));
+  return GBS_OK;
+}
 
 extern "C" const char *gbs_last_error(void) { return gbs::g_last_error.c_str(); }
 

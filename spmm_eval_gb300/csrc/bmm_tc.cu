@@ -31,7 +31,7 @@ namespace gbs {
 constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 128, TC_STAGES = 4;
 constexpr int TC_A_BYTES = TC_BM * TC_BK;  // 16 KiB per stage
 constexpr int TC_B_BYTES = TC_BN * TC_BK;  // 32 KiB per stage
-constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 1024 + 256;
+constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 1024 + 256;  // ring + barriers
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
 
 // kind::f8f6f4 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = E4M3
@@ -202,10 +202,13 @@ __global__ void __launch_bounds__(128, 1)
   }
   __syncwarp();
 
-  // epilogue: warp w owns TMEM lanes (= tile rows) 32w .. 32w + 31
-  const bool have = mbar_wait(accf, 0, a.err);
+  // epilogue: warp w owns TMEM lanes (= tile rows) 32w .. 32w + 31; lane 0
+  // waits and decides for the warp (the TMEM loads need a converged warp)
+  int have = 0;
+  if (lane == 0) have = mbar_wait(accf, 0, a.err) && !s_fail;
+  have = __shfl_sync(0xffffffffu, have, 0);
   tc_fence_after();
-  if (have && !s_fail) {
+  if (have) {
     const int row = m0 + warp * 32 + lane;
     const int Kbits = 32 * a.Kw;
     const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
@@ -243,39 +246,211 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN)
                  : "memory");
   }
 }
 
-// Word-major bits -> K-major e4m3 bytes: out[r][32 kw + b] = bit b of
-// G[kw][r] ? 1.0 : 0.0, columns Kw*32 .. Kp zero.  One thread per (row, word).
-__global__ void k_bits_to_e4m3(const uint32_t *__restrict__ G, int rows, int Kw, int Kp, uint8_t *__restrict__ out) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int words = Kp / 32;
-  if (t >= (long long)rows * words) return;
-  const int kw = (int)(t / rows), r = (int)(t % rows);
-  const uint32_t w = kw < Kw ? __ldg(G + (size_t)kw * rows + r) : 0u;
-  uint32_t o[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    uint32_t x = 0;
-#pragma unroll
-    for (int b = 0; b < 4; ++b) x |= (((w >> (4 * q + b)) & 1u) ? 0x38u : 0u) << (8 * b);
-    o[q] = x;
+// Persistent, warp-specialised version: one CTA per SM walks output tiles
+// tile = blockIdx.x, blockIdx.x + gridDim.x, ...  Warp 0 (one thread) feeds
+// the shared-memory ring with TMA, warp 1 (one thread) issues the MMAs, warps
+// 2-5 drain accumulators.  Tensor memory holds two 128 x 256 FP32
+// accumulators (all 512 columns), so the epilogue of tile i (tcgen05.ld +
+// stores) overlaps the MMAs of tile i + 1.  Barriers: full/empty per ring
+// slot (TMA -> MMA -> TMA), tfull/tempty per accumulator (MMA -> epilogue ->
+// MMA); every wait is bounded.
+__global__ void __launch_bounds__(192, 1)
+    k_bmm_tc_persist(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, BmmTcArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t *sA = base;
+  uint8_t *sB = base + TC_STAGES * TC_A_BYTES;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + TC_STAGES * TC_B_BYTES);
+  uint64_t *empty = full + TC_STAGES;
+  uint64_t *tfull = empty + TC_STAGES;  // [2]
+  uint64_t *tempty = tfull + 2;         // [2]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles_n = (a.N + TC_BN - 1) / TC_BN;
+  const int tiles = tiles_n * ((a.M + TC_BM - 1) / TC_BM);
+  const int nk = a.Kp / TC_BK;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull + b, 1);
+      mbar_init(tempty + b, 4);  // one arrival per epilogue warp
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  uint4 *dst = reinterpret_cast<uint4 *>(out + (size_t)r * Kp + (size_t)kw * 32);
-  dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
-  dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2u * TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;  // k-blocks issued so far (ring position)
+      for (int t = blockIdx.x; t < tiles && !s_fail; t += gridDim.x) {
+        const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * TC_BN;
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % TC_STAGES, r = g / TC_STAGES;
+          if (g >= TC_STAGES && !mbar_wait(empty + s, (uint32_t)((r - 1) & 1), a.err)) {
+            s_fail = 1;
+            break;
+          }
+          mbar_expect_tx(full + s, TC_A_BYTES + TC_B_BYTES);
+          tma_load_2d(sA + s * TC_A_BYTES, &tmA, kb * TC_BK, m0, full + s);
+          tma_load_2d(sB + s * TC_B_BYTES, &tmB, kb * TC_BK, n0, full + s);
+        }
+      }
+      // leave only after the copies in flight have landed
+      for (int q = g - TC_STAGES < 0 ? 0 : g - TC_STAGES; q < g; ++q)
+        if (!mbar_try_wait(full + q % TC_STAGES, (uint32_t)((q / TC_STAGES) & 1)))
+          mbar_wait(full + q % TC_STAGES, (uint32_t)((q / TC_STAGES) & 1), a.err);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int g = 0, i = 0;
+      for (int t = blockIdx.x; t < tiles && !s_fail; t += gridDim.x, ++i) {
+        const int b = i & 1, u = i >> 1;
+        if (u >= 1 && !mbar_wait(tempty + b, (uint32_t)((u - 1) & 1), a.err)) {
+          s_fail = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % TC_STAGES, r = g / TC_STAGES;
+          if (!mbar_wait(full + s, (uint32_t)(r & 1), a.err)) {
+            s_fail = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t ad = sdesc_k_sw128(smem_u32(sA + s * TC_A_BYTES));
+          const uint64_t bd = sdesc_k_sw128(smem_u32(sB + s * TC_B_BYTES));
+#pragma unroll
+          for (int k = 0; k < TC_BK / 32; ++k) mma_f8(acc, ad + 2 * k, bd + 2 * k, TC_IDESC, (kb | k) != 0 ? 1u : 0u);
+          mma_commit(empty + s);
+        }
+        mma_commit(tfull + b);
+        if (s_fail) break;
+      }
+    }
+  } else {
+    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    const int q4 = warp & 3;
+    const int Kbits = 32 * a.Kw;
+    int i = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+      const int b = i & 1, u = i >> 1;
+      // lane 0 waits and decides for the warp, so the .sync.aligned TMEM
+      // loads below run on a converged warp even when a wait gives up
+      int go = 0;
+      if (lane == 0) go = mbar_wait(tfull + b, (uint32_t)(u & 1), a.err) && !s_fail;
+      go = __shfl_sync(0xffffffffu, go, 0);
+      tc_fence_after();
+      if (!go) break;
+      const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * TC_BN;
+      const int row = m0 + q4 * 32 + lane;
+      const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
+#pragma unroll 1
+      for (int cb = 0; cb < TC_BN / 32; ++cb) {
+        uint32_t v[32];
+        tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
+        const int c0 = n0 + cb * 32;
+        if (row < a.M) {
+#pragma unroll
+          for (int q = 0; q < 32; q += 4) {
+            const int c = c0 + q;
+            if (c >= a.N) break;
+            int x[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int andc = (int)__uint_as_float(v[q + e]);
+              int val = andc;
+              if (a.mode != 1) {
+                const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
+                val = a.mode == 0 ? xr : Kbits - 2 * xr;
+              }
+              x[e] = val;
+            }
+            if (a.Cf)
+              *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
+                  make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
+            else
+              *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty + b)) : "memory");
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * TC_BN) : "memory");
+  }
 }
 
-__global__ void k_row_popc_tc(const uint32_t *__restrict__ G, int rows, int Kw, int *__restrict__ p) {
-  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  int s = 0;
-  for (int k = 0; k < Kw; ++k) s += __popc(__ldg(G + (size_t)k * rows + r));
-  p[r] = s;
+// Word-major bits -> K-major e4m3 bytes, plus row popcounts.
+// out[r][32 kw + b] = bit b of G[kw][r] ? 1.0 (0x38) : 0.0, columns Kw*32 ..
+// Kp zero; pop[r] += popc of the row's words (pop zeroed by the caller).  A
+// 256-thread block transposes a 32-word x 32-row tile through shared
+// memory: loads run along rows (contiguous in the word-major input), stores
+// along K (each row's 32 words are 1 KiB contiguous in the output).
+__global__ void __launch_bounds__(256) k_bits_to_e4m3(const uint32_t *__restrict__ G, int rows, int Kw, int Kp,
+                                                      uint8_t *__restrict__ out, int *__restrict__ pop) {
+  __shared__ uint32_t tile[32][33];
+  const int r0 = blockIdx.x * 32, kw0 = blockIdx.y * 32;
+  const int words = Kp / 32;
+  for (int i = threadIdx.x; i < 32 * 32; i += 256) {
+    const int kk = i >> 5, rr = i & 31;
+    const int kw = kw0 + kk, r = r0 + rr;
+    tile[kk][rr] = (kw < Kw && r < rows) ? __ldg(G + (size_t)kw * rows + r) : 0u;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && r0 + (int)threadIdx.x < rows && kw0 < Kw) {
+    int c = 0;
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) c += __popc(tile[kk][threadIdx.x]);
+    atomicAdd(pop + r0 + threadIdx.x, c);
+  }
+  // 32 rows x 32 words x 2 halves of 16 bits -> 16-byte stores
+  for (int i = threadIdx.x; i < 32 * 64; i += 256) {
+    const int rr = i >> 6, q = i & 63, kk = q >> 1, h = q & 1;
+    const int r = r0 + rr, kw = kw0 + kk;
+    if (r >= rows || kw >= words) continue;
+    const uint32_t w = tile[kk][rr] >> (16 * h);
+    uint32_t o[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      // spread the 4 bits of a nibble to the low bit of 4 bytes (bit b ->
+      // bit 8b; the four shifted copies occupy disjoint bit ranges, so the
+      // product has no carries), then scale each 0/1 byte to 0x38
+      const uint32_t nib = (w >> (4 * n)) & 0xFu;
+      o[n] = ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+    }
+    *reinterpret_cast<uint4 *>(out + (size_t)r * Kp + (size_t)kw * 32 + h * 16) = make_uint4(o[0], o[1], o[2], o[3]);
+  }
 }
 
 namespace {
@@ -313,7 +488,7 @@ gbs_status make_map(CUtensorMap *map, void *base, int rows, int Kp, int box_rows
 static __device__ int g_bmm_tc_err;
 
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
-                      int ldc, cudaStream_t s) {
+                      int ldc, cudaStream_t s, bool persistent) {
   GBS_REQUIRE(M % 4 == 0 && N % 4 == 0 && ldc % 4 == 0, "bmm tc: M, N (and ldc) must be multiples of 4");
   GBS_REQUIRE((long long)Kw * 32 < (1ll << 24), "bmm tc: K must be < 2^24 bits (exact FP32 accumulation)");
   const int Kp = (Kw * 32 + TC_BK - 1) / TC_BK * TC_BK;
@@ -322,11 +497,11 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   GBS_TRY(B8.alloc((size_t)N * Kp, s));
   GBS_TRY(pa.alloc(sizeof(int) * (size_t)M, s));
   GBS_TRY(pb.alloc(sizeof(int) * (size_t)N, s));
-  const long long ta = (long long)M * (Kp / 32), tb = (long long)N * (Kp / 32);
-  k_bits_to_e4m3<<<(int)((ta + 255) / 256), 256, 0, s>>>(A, M, Kw, Kp, A8.as<uint8_t>());
-  k_bits_to_e4m3<<<(int)((tb + 255) / 256), 256, 0, s>>>(B, N, Kw, Kp, B8.as<uint8_t>());
-  k_row_popc_tc<<<(M + 255) / 256, 256, 0, s>>>(A, M, Kw, pa.as<int>());
-  k_row_popc_tc<<<(N + 255) / 256, 256, 0, s>>>(B, N, Kw, pb.as<int>());
+  GBS_CUDA_TRY(cudaMemsetAsync(pa.p, 0, sizeof(int) * (size_t)M, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(pb.p, 0, sizeof(int) * (size_t)N, s));
+  const int wb = (Kp / 32 + 31) / 32;
+  k_bits_to_e4m3<<<dim3((M + 31) / 32, wb), 256, 0, s>>>(A, M, Kw, Kp, A8.as<uint8_t>(), pa.as<int>());
+  k_bits_to_e4m3<<<dim3((N + 31) / 32, wb), 256, 0, s>>>(B, N, Kw, Kp, B8.as<uint8_t>(), pb.as<int>());
   GBS_TRY(check_launch("bmm tc prologue"));
   CUtensorMap ma, mb;
   GBS_TRY(make_map(&ma, A8.p, M, Kp, TC_BM));
@@ -335,13 +510,23 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
     attr_err = cudaFuncSetAttribute(k_bmm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_bmm_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   });
   if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(k_bmm_tc)");
   int *err = nullptr;
   GBS_CUDA_TRY(cudaGetSymbolAddress((void **)&err, g_bmm_tc_err));
   BmmTcArgs args{M, N, Kw, Kp, mode, pa.as<int>(), pb.as<int>(), C, Cf, ldc, err};
-  dim3 grid((N + TC_BN - 1) / TC_BN, (M + TC_BM - 1) / TC_BM);
-  k_bmm_tc<<<grid, 128, TC_SMEM, s>>>(ma, mb, args);
+  const int tiles = ((N + TC_BN - 1) / TC_BN) * ((M + TC_BM - 1) / TC_BM);
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  if (persistent) {
+    const int grid = tiles < di.sm_count ? tiles : di.sm_count;
+    k_bmm_tc_persist<<<grid, 192, TC_SMEM, s>>>(ma, mb, args);
+  } else {
+    dim3 grid((N + TC_BN - 1) / TC_BN, (M + TC_BM - 1) / TC_BM);
+    k_bmm_tc<<<grid, 128, TC_SMEM, s>>>(ma, mb, args);
+  }
   return check_launch("k_bmm_tc");
 }
 

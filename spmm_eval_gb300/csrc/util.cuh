@@ -18,8 +18,17 @@ inline int bits_for(long long v) {
   return b;
 }
 
-// RAII device buffer from stream-ordered allocation (freed on the same
-// stream).  Used only where an entry point documents that it allocates.
+// The library's own stream-ordered memory pool on the current device.  It
+// keeps up to kPoolKeepBytes of freed temporaries mapped across
+// synchronisations, so back-to-back calls do not pay for mapping fresh
+// memory each time (the device's default pool returns everything at every
+// synchronisation).  gbs_pool_trim releases what it keeps.
+constexpr unsigned long long kPoolKeepBytes = 8ull << 30;
+gbs_status lib_pool(cudaMemPool_t *out);
+
+// RAII device buffer from stream-ordered allocation in the library pool
+// (freed on the same stream).  Used only where an entry point documents that
+// it allocates.
 struct DevBuf {
   void *p = nullptr;
   cudaStream_t s = nullptr;
@@ -29,10 +38,12 @@ struct DevBuf {
   gbs_status alloc(size_t bytes, cudaStream_t stream) {
     s = stream;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+    cudaMemPool_t pool;
+    GBS_TRY(lib_pool(&pool));
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
     if (e != cudaSuccess) {
       p = nullptr;
-      return cuda_fail(e, "cudaMallocAsync");
+      return cuda_fail(e, "cudaMallocFromPoolAsync");
     }
     return GBS_OK;
   }

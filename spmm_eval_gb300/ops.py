@@ -313,7 +313,7 @@ def b2sr_aligned(Ab: B2SR):
 # Dense binary matmul (word-major operands, ToBit32ColUd layout)
 # ---------------------------------------------------------------------------
 BMM_XOR, BMM_AND, BMM_SIGNED = 0, 1, 2
-BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA, BMM_ALGO_TC = 0, 1, 2, 3
+BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA, BMM_ALGO_TC, BMM_ALGO_TC_PERSIST = 0, 1, 2, 3, 4
 
 
 def bmm_tc_timeouts() -> int:
@@ -438,6 +438,12 @@ def sddmm(A: CSR, G: torch.Tensor, H: torch.Tensor, out: torch.Tensor | None = N
 # ---------------------------------------------------------------------------
 # Matrix Market ingest (host)
 # ---------------------------------------------------------------------------
+def pool_trim() -> None:
+    """Return the unused memory of the library's temporaries pool on the
+    current device (gbs_pool_trim)."""
+    _lib.call("gbs_pool_trim")
+
+
 def read_mtx(path: str):
     """(nrows, ncols, rowptr, colind, vals) as numpy arrays, with the
     reference's readMtx + coo2csr semantics."""
