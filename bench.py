@@ -322,11 +322,15 @@ def run_ours(args):
     dvals = torch.empty_like(g.vals)
     Apat = ops.CSR(g.rowptr, g.colind, None, n, n)
 
+    # planned fused backward: A^T dY and SDDMM(dY, H) in one pass over each
+    # row-range piece of A^T (pieces chosen so the dY slice fits in L2)
+    bplans = {torch.float32: ops.BackwardPlan(T, t_vals, F, torch.float32),
+              torch.bfloat16: ops.BackwardPlan(T, t_vals, F, torch.bfloat16)}
+
     def fwd_bwd(Hx, Gx, Cx):
         pf = plan32 if Hx.dtype == torch.float32 else plan16
         pf.run(Hx, out=Cx, workspace=ws)
-        # fused backward: A^T dY and SDDMM(dY, H) in one pass over A^T
-        ops.spmm_backward(T, t_vals, Gx, Hx, dB=dH, dvals=dvals, workspace=ws)
+        bplans[Hx.dtype].run(Gx, Hx, dB=dH, dvals=dvals, workspace=ws)
 
     for _ in range(3):
         fwd_bwd(B, Gd, C)
@@ -394,7 +398,9 @@ def run_ours(args):
                      "traffic": traffic, "peak_source": peak_kind,
                      "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per launch",
                      "bytes_per_launch": bytes_f32},
-        "fwd_bwd": {"what": "planned SpMM A H + fused backward (A^T dY and SDDMM(dY, H) in one pass), F=256",
+        "fwd_bwd": {"what": "planned SpMM A H + planned fused backward (A^T dY and SDDMM(dY, H) in one pass "
+                            "per row-range piece of A^T), F=256",
+                    "backward_parts": {"f32": bplans[torch.float32].parts, "bf16": bplans[torch.bfloat16].parts},
                     "f32_ms": round(ms_fb32, 4), "bf16_ms": round(ms_fb16, 4),
                     "bf16_speedup": round(ms_fb32 / ms_fb16, 3)},
         "bf16": {"ms_per_step": round(ms_bf16, 4),
@@ -423,11 +429,13 @@ def run_profile_case(args):
       full   : bench graph, FP32 then BF16 planned merge-path SpMM, F = 256
                (FP32: 4 column parts = 4 launches per step)
       eighth : same nodes (B still larger than L2), 1/8 of the degree
-      fwdbwd : eighth graph, SpMM + A^T SpMM + SDDMM (FP32, then BF16)
+      fwdbwd : eighth graph, planned SpMM + planned fused backward (FP32, then
+               BF16)
       b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
                B2SR BMM F = 256
       bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 per tile, tcgen05
-               persistent (XOR counts)"""
+               persistent (XOR counts)
+      bmmtc  : 8192^3 binary GEMM, default (persistent tcgen05) only"""
     import torch
     from spmm_eval_gb300 import graphs as G
     from spmm_eval_gb300 import ops
@@ -452,14 +460,16 @@ def run_profile_case(args):
             Gh = Gd.to(torch.bfloat16)
             dH = torch.empty_like(C)
             dv = torch.empty_like(g.vals)
-            Ap = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
             torch.cuda.synchronize()
             torch.cuda.empty_cache()
+            plans = {dt: (ops.SpmmPlan(A, 256, dt), ops.BackwardPlan(T, tv, 256, dt))
+                     for dt in (torch.float32, torch.bfloat16)}
             for Hx, Gx in ((B, Gd), (Bh, Gh)):
+                pf, pb = plans[Hx.dtype]
                 for _ in range(2 + args.steps):
-                    ops.csr_spmm(A, Hx, out=C, workspace=ws)
-                    T.spmm(tv, Gx, out=dH, workspace=ws)
-                    ops.sddmm(Ap, Gx, Hx, out=dv)
+                    pf.run(Hx, out=C, workspace=ws)
+                    pb.run(Gx, Hx, dB=dH, dvals=dv, workspace=ws)
+            out["parts"] = {str(k): [v[0].parts, v[1].parts] for k, v in plans.items()}
         else:
             plans = {torch.float32: ops.SpmmPlan(A, 256, torch.float32),
                      torch.bfloat16: ops.SpmmPlan(A, 256, torch.bfloat16)}
@@ -482,14 +492,16 @@ def run_profile_case(args):
         for _ in range(2 + args.steps):
             ops.b2sr_bmm(Ab, Xw, 256)
         out.update(nodes=g.nrows, nnz=g.nnz, nnzb=Ab.nnzb)
-    elif case == "bmm":
+    elif case in ("bmm", "bmmtc"):
         gen = torch.Generator(device=dev)
         gen.manual_seed(0)
-        Kw, M = 128, 4096
+        Kw, M = (128, 4096) if case == "bmm" else (256, 8192)
         Aw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Bw = torch.randint(-2**31, 2**31 - 1, (Kw, M), dtype=torch.int32, device=dev, generator=gen)
         Co = torch.empty((M, M), dtype=torch.int32, device=dev)
-        for algo in (ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA, ops.BMM_ALGO_TC, ops.BMM_ALGO_TC_PERSIST):
+        algos = ((ops.BMM_ALGO_POPC, ops.BMM_ALGO_MMA, ops.BMM_ALGO_TC, ops.BMM_ALGO_TC_PERSIST)
+                 if case == "bmm" else (ops.BMM_ALGO_DEFAULT,))
+        for algo in algos:
             for _ in range(2 + args.steps):
                 ops.bmm_b1(Aw, Bw, ops.BMM_XOR, algo, out=Co)
     torch.cuda.synchronize()
@@ -504,7 +516,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "b2sr", "bmm"], default=None,
+    ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "b2sr", "bmm", "bmmtc"], default=None,
                     help="run a short fixed launch sequence for ncu instead of the bench")
     args = ap.parse_args()
     if args.profile_case:

@@ -207,6 +207,31 @@ GBS_API gbs_status gbs_spmm_backward(const gbs_csr_transpose *T, const float *d_
                              const void *d_dC, const void *d_H, gbs_dtype dtype,
                              int F, float *d_dB, float *d_dvals, void *d_workspace,
                              size_t workspace_bytes, gbs_stream_t stream);
+/* Planned fused backward: A^T split by column ranges (= row ranges of A,
+ * slices of dC) into `parts` pieces (0 = automatic: the fewest whose dC
+ * slice fits in half of L2, 1 while dC already does) so that every pass's
+ * dC gathers stay in L2; the dB part of each pass accumulates and every
+ * entry's dvals comes from the one pass holding it.  The plan copies the
+ * pieces of T's arrays and of t_vals (NULL: binary A) at creation and
+ * synchronises the stream; with 1 part it keeps pointers to T's arrays and
+ * t_vals, which must then outlive it.  Recreate it when the values change.
+ * No counterpart in the reference (its repo has no backward). */
+typedef struct gbs_spmm_backward_plan gbs_spmm_backward_plan;
+GBS_API gbs_status gbs_spmm_backward_plan_create(const gbs_csr_transpose *T,
+                                         const float *d_t_vals, gbs_dtype dtype,
+                                         int F, int parts, gbs_stream_t stream,
+                                         gbs_spmm_backward_plan **out);
+GBS_API gbs_status gbs_spmm_backward_plan_parts(const gbs_spmm_backward_plan *plan,
+                                        int *parts);
+GBS_API gbs_status gbs_spmm_backward_plan_destroy(gbs_spmm_backward_plan *plan);
+/* Same results as gbs_spmm_backward (dB to FP32 rounding of a different
+ * summation split, dvals bitwise when the dot products' lane order is
+ * unchanged); workspace as gbs_spmm_backward. */
+GBS_API gbs_status gbs_spmm_backward_planned(const gbs_spmm_backward_plan *plan,
+                                     const void *d_dC, const void *d_H,
+                                     float *d_dB, float *d_dvals,
+                                     void *d_workspace, size_t workspace_bytes,
+                                     gbs_stream_t stream);
 /* out[e] = sum_k G[row(e)][k] * H[col(e)][k], FP32 accumulation; G nrows x F
  * and H ncols x F in dtype. */
 GBS_API gbs_status gbs_sddmm(int nrows, int ncols, int nnz, const int *d_rowptr,

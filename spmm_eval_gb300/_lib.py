@@ -64,6 +64,10 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_csr_transpose_destroy": (st, [p]),
     "gbs_csr_spmm_transposed": (st, [p, p, p, i32, i32, p, p, sz, p]),
     "gbs_spmm_backward": (st, [p, p, p, p, i32, i32, p, p, p, sz, p]),
+    "gbs_spmm_backward_plan_create": (st, [p, p, i32, i32, i32, p, C.POINTER(p)]),
+    "gbs_spmm_backward_plan_parts": (st, [p, pi32]),
+    "gbs_spmm_backward_plan_destroy": (st, [p]),
+    "gbs_spmm_backward_planned": (st, [p, p, p, p, p, p, sz, p]),
     "gbs_sddmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr2b2sr_nnzb": (st, [i32, i32, i32, p, p, i32, p, pi32, p]),
     "gbs_csr2b2sr": (st, [i32, i32, i32, p, p, i32, p, p, p, p]),

@@ -253,6 +253,21 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// Grouped tile order of the persistent kernel: tiles run in groups of
+// TC_GROUP_M tile rows, down the group's rows first and across N second, so
+// the CTAs resident at any moment share a few A row-blocks and a few B
+// column-blocks; both stay in L2 across consecutive tiles instead of all of
+// B being re-read from DRAM for every wave of tiles.
+constexpr int TC_GROUP_M = 16;
+__device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int *m0, int *n0) {
+  const int per_group = TC_GROUP_M * tiles_n;
+  const int grp = t / per_group, first = grp * TC_GROUP_M;
+  const int gm = tiles_m - first < TC_GROUP_M ? tiles_m - first : TC_GROUP_M;
+  const int local = t - grp * per_group;
+  *m0 = (first + local % gm) * TC_BM;
+  *n0 = (local / gm) * TC_BN;
+}
+
 // Persistent, warp-specialised version: one CTA per SM walks output tiles
 // tile = blockIdx.x, blockIdx.x + gridDim.x, ...  Warp 0 (one thread) feeds
 // the shared-memory ring with TMA, warp 1 (one thread) issues the MMAs, warps
@@ -275,8 +290,8 @@ __global__ void __launch_bounds__(192, 1)
   __shared__ int s_fail;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_n = (a.N + TC_BN - 1) / TC_BN;
-  const int tiles = tiles_n * ((a.M + TC_BM - 1) / TC_BM);
+  const int tiles_n = (a.N + TC_BN - 1) / TC_BN, tiles_m = (a.M + TC_BM - 1) / TC_BM;
+  const int tiles = tiles_n * tiles_m;
   const int nk = a.Kp / TC_BK;
 
   if (threadIdx.x == 0) {
@@ -306,7 +321,8 @@ __global__ void __launch_bounds__(192, 1)
     if (lane == 0) {
       int g = 0;  // k-blocks issued so far (ring position)
       for (int t = blockIdx.x; t < tiles && !s_fail; t += gridDim.x) {
-        const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * TC_BN;
+        int m0, n0;
+        tile_origin(t, tiles_m, tiles_n, &m0, &n0);
         for (int kb = 0; kb < nk; ++kb, ++g) {
           const int s = g % TC_STAGES, r = g / TC_STAGES;
           if (g >= TC_STAGES && !mbar_wait(empty + s, (uint32_t)((r - 1) & 1), a.err)) {
@@ -365,7 +381,8 @@ __global__ void __launch_bounds__(192, 1)
       go = __shfl_sync(0xffffffffu, go, 0);
       tc_fence_after();
       if (!go) break;
-      const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * TC_BN;
+      int m0, n0;
+      tile_origin(t, tiles_m, tiles_n, &m0, &n0);
       const int row = m0 + q4 * 32 + lane;
       const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
 #pragma unroll 1

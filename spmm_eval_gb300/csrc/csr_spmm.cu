@@ -43,14 +43,28 @@ SpmmVariant mk() {
   return SpmmVariant{(const void *)&k_csr_spmm_merge<DT, VEC, LPR, CH, U, MINB>, VEC, LPR, CH};
 }
 
+// Lanes per row (LPR) and 16-byte chunks per lane (CH) for rows of nvec
+// chunks.  With `halfwarp` (the gathered rows of B fit in half of L2), rows
+// of 17-32 chunks of 16-bit features and 33-64 chunks of FP32 (F = 136..256)
+// run on half-warps, two nonzeros per warp at a time: one shuffle pair then
+// feeds two gathers, which measured 4.8 against 5.3 ms (BF16, 2 parts) and
+// 6.4 against 6.7 ms (FP32, 4 parts) on the 114.8M-edge graph at F = 256.
+// The half-warp variants need more registers (3 instead of 4 CTAs per SM),
+// which costs more than it saves when many gathers go to DRAM.
 template <int DT, int VEC>
-bool pick_lpr_ch(int nvec, SpmmVariant *v) {
+bool pick_lpr_ch(int nvec, bool halfwarp, SpmmVariant *v) {
   if (nvec <= 1) { *v = mk<DT, VEC, 1, 1>(); return true; }
   if (nvec <= 2) { *v = mk<DT, VEC, 2, 1>(); return true; }
   if (nvec <= 4) { *v = mk<DT, VEC, 4, 1>(); return true; }
   if (nvec <= 8) { *v = mk<DT, VEC, 8, 1>(); return true; }
   if (nvec <= 16) { *v = mk<DT, VEC, 16, 1>(); return true; }
+  if constexpr (VEC == 8) {
+    if (halfwarp && nvec <= 32) { *v = mk<DT, VEC, 16, 2>(); return true; }
+  }
   if (nvec <= 32) { *v = mk<DT, VEC, 32, 1>(); return true; }
+  if constexpr (VEC == 4) {
+    if (halfwarp && nvec <= 64) { *v = mk<DT, VEC, 16, 4>(); return true; }
+  }
   if (nvec <= 64) { *v = mk<DT, VEC, 32, 2>(); return true; }
   if (nvec <= 128) { *v = mk<DT, VEC, 32, 4>(); return true; }
   if (nvec <= 256) { *v = mk<DT, VEC, 32, 8>(); return true; }
@@ -67,17 +81,18 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 // Variant for a column block of width Fw.  vec16 = 16-byte vector loads are
 // allowed (aligned pointers, F a multiple of the vector width).
-gbs_status spmm_select(int dt, int Fw, bool vec16, SpmmVariant *out) {
+gbs_status spmm_select(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out) {
   bool ok = false;
   if (dt == DT_F32) {
-    if (vec16 && Fw % 4 == 0) ok = pick_lpr_ch<DT_F32, 4>(Fw / 4, out);
-    else ok = pick_lpr_ch<DT_F32, 1>(Fw, out);
+    if (vec16 && Fw % 4 == 0) ok = pick_lpr_ch<DT_F32, 4>(Fw / 4, halfwarp, out);
+    else ok = pick_lpr_ch<DT_F32, 1>(Fw, halfwarp, out);
     if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: FP32 features need F <= 1024");
   } else {
     if (!vec16 || Fw % 8 != 0)
       return fail(GBS_ERR_UNSUPPORTED,
                   "csr spmm: 16-bit features need F % 8 == 0 and 16-byte aligned B/C");
-    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(Fw / 8, out) : pick_lpr_ch<DT_F16, 8>(Fw / 8, out);
+    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(Fw / 8, halfwarp, out)
+                       : pick_lpr_ch<DT_F16, 8>(Fw / 8, halfwarp, out);
     if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: 16-bit features need F <= 2048");
   }
   return GBS_OK;
@@ -194,11 +209,14 @@ gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, con
 }
 
 gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B, const float *C,
-                     int col_block, SpmmPlan *p) {
+                     int col_block, SpmmPlan *p, int gathered_rows) {
   const int vec = dt == DT_F32 ? 4 : 8;
   p->vec16 = aligned16(B) && aligned16(C) && F % vec == 0;
   GBS_TRY(spmm_col_block(dt, ncols, nnz, F, p->vec16, col_block, &p->Fw));
-  GBS_TRY(spmm_select(dt, p->Fw, p->vec16, &p->v));
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  const double slice = (double)(gathered_rows >= 0 ? gathered_rows : ncols) * p->Fw * (dt == DT_F32 ? 4 : 2);
+  GBS_TRY(spmm_select(dt, p->Fw, p->vec16, slice <= 0.5 * (double)di.l2_bytes, &p->v));
   GBS_TRY(spmm_warps(p->v, nrows, nnz, &p->P));
   p->nblk = F / p->Fw;
   p->esize = dt == DT_F32 ? 4 : 2;
@@ -214,14 +232,19 @@ gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes
     if (dt != DT_F32 && !vec16) continue;
     for (int Fw = 1; Fw <= F; ++Fw) {
       if (F % Fw != 0) continue;
-      SpmmVariant v;
-      if (spmm_select(dt, Fw, vec16 != 0, &v) != GBS_OK) { clear_error(); continue; }
-      int P = 1;
-      GBS_TRY(spmm_warps(v, nrows, nnz, &P));
-      size_t b = spmm_workspace_bytes(P, Fw);
-      if (b > best) best = b;
+      for (int hw = 0; hw < 2; ++hw) {
+        SpmmVariant v;
+        if (spmm_select(dt, Fw, vec16 != 0, hw != 0, &v) != GBS_OK) { clear_error(); continue; }
+        int P = 1;
+        GBS_TRY(spmm_warps(v, nrows, nnz, &P));
+        size_t b = spmm_workspace_bytes(P, Fw);
+        if (b > best) best = b;
+      }
     }
   }
+  size_t bb = 0;
+  GBS_TRY(bwd_workspace_bytes(dt, nrows, nnz, F, &bb));
+  if (bb > best) best = bb;
   *bytes = best;
   return GBS_OK;
 }

@@ -45,7 +45,77 @@ bool pickb(int nvec, SpmmVariant *v) {
 }
 
 }  // namespace
+
+gbs_status bwd_variant(gbs_dtype dtype, int F, SpmmVariant *v, int *dt) {
+  GBS_REQUIRE(dtype == GBS_F32 || dtype == GBS_BF16 || dtype == GBS_F16, "spmm backward: bad dtype");
+  GBS_REQUIRE(F >= 1, "spmm backward: F must be >= 1");
+  *dt = dtype == GBS_F32 ? DT_F32 : (dtype == GBS_BF16 ? DT_BF16 : DT_F16);
+  const int vec = *dt == DT_F32 ? 4 : 8;
+  GBS_REQUIRE(F % vec == 0, "spmm backward: F must be a multiple of 4 (FP32) / 8 (16-bit)");
+  bool ok = *dt == DT_F32 ? pickb<DT_F32, 4>(F / 4, v)
+                          : (*dt == DT_BF16 ? pickb<DT_BF16, 8>(F / 8, v) : pickb<DT_F16, 8>(F / 8, v));
+  if (!ok) return fail(GBS_ERR_UNSUPPORTED, "spmm backward: F too large (FP32 <= 1024, 16-bit <= 2048)");
+  return GBS_OK;
+}
+
+gbs_status bwd_launch(const SpmmVariant &v, int n, int nnz, const int *rowptr, const int *colind, const float *vals,
+                      const int *perm, const void *dC, const void *H, int F, float *dB, float *dvals, void *ws,
+                      size_t ws_bytes, int accumulate, cudaStream_t s) {
+  int P = 0;
+  GBS_TRY(spmm_warps(v, n, nnz, &P));
+  GBS_REQUIRE(ws != nullptr && ws_bytes >= spmm_workspace_bytes(P, F),
+              "spmm backward: workspace missing or too small (size it as gbs_csr_spmm_workspace_size(ncols, nnz, F))");
+  MergeArgs a;
+  a.nrows = n;
+  a.nnz = nnz;
+  a.F = F;
+  a.nvec = F / v.vec;
+  a.ldb = F;
+  a.ldc = F;
+  a.rowptr = rowptr;
+  a.rp_base = 0;
+  a.colind = colind;
+  a.vals = vals;
+  a.B = dC;
+  a.C = dB;
+  a.ldp = (int)align_up((size_t)F, 4);
+  a.P = P;
+  const long long total = (long long)n + nnz;
+  a.D = (total + P - 1) / P;
+  if (a.D < 1) a.D = 1;
+  a.counters = reinterpret_cast<int *>(ws);
+  a.partials = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + spmm_counter_bytes());
+  a.accumulate = accumulate;
+  a.H = H;
+  a.dvals = dvals;
+  a.perm = perm;
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3((unsigned)((P * 32 + 255) / 256)), dim3(256), args, 0, s));
+  return GBS_OK;
+}
+
+gbs_status bwd_workspace_bytes(int dt, int nrows, int nnz, int F, size_t *bytes) {
+  *bytes = 0;
+  const gbs_dtype d = dt == DT_F32 ? GBS_F32 : (dt == DT_BF16 ? GBS_BF16 : GBS_F16);
+  SpmmVariant v{};
+  int dd = 0;
+  if (bwd_variant(d, F, &v, &dd) != GBS_OK) {  // no backward kernel for this shape
+    clear_error();
+    return GBS_OK;
+  }
+  int P = 0;
+  GBS_TRY(spmm_warps(v, nrows, nnz, &P));
+  *bytes = spmm_workspace_bytes(P, F);
+  return GBS_OK;
+}
+
 }  // namespace gbs
+
+struct gbs_spmm_backward_plan {
+  int n, nnz, F;  // rows of A^T (= columns of A), entries
+  gbs_dtype dtype;
+  gbs::ColumnParts parts;  // A^T by column ranges; extra = transpose permutation
+};
 
 using namespace gbs;
 
@@ -54,51 +124,80 @@ extern "C" gbs_status gbs_spmm_backward(const gbs_csr_transpose *T, const float 
                                         size_t ws_bytes, gbs_stream_t stream) {
   clear_error();
   GBS_REQUIRE(T != nullptr, "spmm backward: null transpose handle");
-  GBS_REQUIRE(dtype == GBS_F32 || dtype == GBS_BF16 || dtype == GBS_F16, "spmm backward: bad dtype");
-  GBS_REQUIRE(F >= 1, "spmm backward: F must be >= 1");
+  SpmmVariant v{};
+  int dt = 0;
+  GBS_TRY(bwd_variant(dtype, F, &v, &dt));
   const int n = T->ncols;  // rows of A^T
   if (n == 0) return GBS_OK;
   GBS_REQUIRE(dC && H && dB && dvals, "spmm backward: null pointer");
-  const int dt = dtype == GBS_F32 ? DT_F32 : (dtype == GBS_BF16 ? DT_BF16 : DT_F16);
   const uintptr_t al = reinterpret_cast<uintptr_t>(dC) | reinterpret_cast<uintptr_t>(H) |
                        reinterpret_cast<uintptr_t>(dB);
-  const int vec = dt == DT_F32 ? 4 : 8;
-  GBS_REQUIRE((al & 15u) == 0 && F % vec == 0,
-              "spmm backward: needs 16-byte aligned dC, H, dB and F a multiple of 4 (FP32) / 8 (16-bit)");
+  GBS_REQUIRE((al & 15u) == 0, "spmm backward: needs 16-byte aligned dC, H and dB");
+  return bwd_launch(v, n, T->nnz, T->t_rowptr, T->t_colind, t_vals, T->perm, dC, H, F, dB, dvals, ws, ws_bytes, 0,
+                    (cudaStream_t)stream);
+}
+
+extern "C" gbs_status gbs_spmm_backward_plan_create(const gbs_csr_transpose *T, const float *t_vals,
+                                                    gbs_dtype dtype, int F, int parts, gbs_stream_t stream,
+                                                    gbs_spmm_backward_plan **out) {
+  clear_error();
+  GBS_REQUIRE(out != nullptr, "spmm backward plan: null output");
+  *out = nullptr;
+  GBS_REQUIRE(T != nullptr, "spmm backward plan: null transpose handle");
+  GBS_REQUIRE(parts >= 0 && parts <= 64, "spmm backward plan: parts must be 0 (auto) .. 64");
   SpmmVariant v{};
-  bool ok = dt == DT_F32 ? pickb<DT_F32, 4>(F / 4, &v)
-                         : (dt == DT_BF16 ? pickb<DT_BF16, 8>(F / 8, &v) : pickb<DT_F16, 8>(F / 8, &v));
-  if (!ok) return fail(GBS_ERR_UNSUPPORTED, "spmm backward: F too large (FP32 <= 1024, 16-bit <= 2048)");
-  int P = 0;
-  GBS_TRY(spmm_warps(v, n, T->nnz, &P));
-  GBS_REQUIRE(ws != nullptr && ws_bytes >= spmm_workspace_bytes(P, F),
-              "spmm backward: workspace missing or too small (size it as gbs_csr_spmm_workspace_size(ncols, nnz, F))");
-  MergeArgs a;
-  a.nrows = n;
-  a.nnz = T->nnz;
-  a.F = F;
-  a.nvec = F / v.vec;
-  a.ldb = F;
-  a.ldc = F;
-  a.rowptr = T->t_rowptr;
-  a.rp_base = 0;
-  a.colind = T->t_colind;
-  a.vals = t_vals;
-  a.B = dC;
-  a.C = dB;
-  a.ldp = (int)align_up((size_t)F, 4);
-  a.P = P;
-  const long long total = (long long)n + T->nnz;
-  a.D = (total + P - 1) / P;
-  if (a.D < 1) a.D = 1;
-  a.counters = reinterpret_cast<int *>(ws);
-  a.partials = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + spmm_counter_bytes());
-  a.accumulate = 0;
-  a.H = H;
-  a.dvals = dvals;
-  a.perm = T->perm;
-  void *args[] = {&a};
-  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3((unsigned)((P * 32 + 255) / 256)), dim3(256), args, 0,
-                                (cudaStream_t)stream));
+  int dt = 0;
+  GBS_TRY(bwd_variant(dtype, F, &v, &dt));
+  int K = parts;
+  // the gathered operand is dC: rows of A x F
+  if (K == 0) GBS_TRY(auto_parts((double)T->nrows * F * (dtype == GBS_F32 ? 4.0 : 2.0), T->nnz, T->nrows, &K));
+  auto *P = new gbs_spmm_backward_plan();
+  P->n = T->ncols;
+  P->nnz = T->nnz;
+  P->F = F;
+  P->dtype = dtype;
+  gbs_status st = partition_columns(T->ncols, T->nrows, T->nnz, T->t_rowptr, T->t_colind, t_vals, T->perm, K,
+                                    (cudaStream_t)stream, &P->parts);
+  if (st != GBS_OK) {
+    delete P;
+    return st;
+  }
+  *out = P;
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_spmm_backward_plan_parts(const gbs_spmm_backward_plan *P, int *parts) {
+  clear_error();
+  GBS_REQUIRE(P && parts, "spmm backward plan: null argument");
+  *parts = P->parts.K;
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_spmm_backward_plan_destroy(gbs_spmm_backward_plan *P) {
+  clear_error();
+  if (P) {
+    P->parts.release();
+    delete P;
+  }
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_spmm_backward_planned(const gbs_spmm_backward_plan *P, const void *dC, const void *H,
+                                                float *dB, float *dvals, void *ws, size_t ws_bytes,
+                                                gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(P != nullptr, "spmm backward planned: null plan");
+  if (P->n == 0) return GBS_OK;
+  GBS_REQUIRE(dC && H && dB && dvals, "spmm backward planned: null pointer");
+  const uintptr_t al = reinterpret_cast<uintptr_t>(dC) | reinterpret_cast<uintptr_t>(H) |
+                       reinterpret_cast<uintptr_t>(dB);
+  GBS_REQUIRE((al & 15u) == 0, "spmm backward planned: needs 16-byte aligned dC, H and dB");
+  SpmmVariant v{};
+  int dt = 0;
+  GBS_TRY(bwd_variant(P->dtype, P->F, &v, &dt));
+  const ColumnParts &cp = P->parts;
+  for (int p = 0; p < cp.K; ++p)
+    GBS_TRY(bwd_launch(v, P->n, cp.nnz[p], cp.rowptr[p], cp.colind[p], cp.vals[p], cp.extra[p], dC, H, P->F, dB,
+                       dvals, ws, ws_bytes, p > 0 ? 1 : 0, (cudaStream_t)stream));
   return GBS_OK;
 }

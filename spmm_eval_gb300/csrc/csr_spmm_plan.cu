@@ -1,12 +1,14 @@
 // Column-partitioned CSR SpMM plan.
 //
-// When the feature matrix B is larger than L2 (FP32 B of the 232,965-node
-// graph at F = 256 is 238 MB against 129 MB of L2), a quarter of the row
-// gathers miss L2.  Splitting A by column ranges into K parts whose slices of
-// B fit in half of L2, and running the merge-path SpMM once per part with the
-// later parts accumulating into C (C += A_p B_p), keeps every pass's gathers
-// in L2 at the price of reading and writing C K-1 more times.  Measured on
-// GB300 for that graph: 8.0 ms in one pass, 6.6 ms as 4 parts.
+// When the feature matrix B is larger than half of L2 (FP32 B of the
+// 232,965-node graph at F = 256 is 238 MB, BF16 119 MB, against 129 MB of
+// L2 split over two dies), many row gathers miss L2.  Splitting A by column
+// ranges into K parts whose slices of B fit in half of L2, and running the
+// merge-path SpMM once per part with the later parts accumulating into C
+// (C += A_p B_p), keeps every pass's gathers in L2 at the price of reading
+// and writing C K-1 more times.  Measured on GB300 for that graph: FP32
+// 8.0 ms in one pass, 6.4 ms as 4 parts; BF16 5.4 ms in one pass, 4.8 ms as
+// 2 parts.
 //
 // The plan copies A into the K parts once (rows in the same order, each
 // part's columns still ascending); it is reused for any B of the planned
@@ -19,13 +21,9 @@
 #include "util.cuh"
 
 struct gbs_csr_spmm_plan {
-  int nrows, ncols, nnz, F, K;
+  int nrows, ncols, nnz, F;
   gbs_dtype btype;
-  int device;
-  bool owned;
-  std::vector<int *> rowptr, colind;
-  std::vector<float *> vals;
-  std::vector<int> part_nnz;
+  gbs::ColumnParts parts;
 };
 
 namespace gbs {
@@ -62,8 +60,9 @@ __global__ void k_part_bounds(const int *__restrict__ rowptr, const int *__restr
 
 // Warp per row: copy each column range to its part.
 __global__ void k_part_copy(const int *__restrict__ rowptr, const int *__restrict__ colind,
-                            const float *__restrict__ vals, int nrows, int K, int *const *__restrict__ prp,
-                            int *const *__restrict__ pci, float *const *__restrict__ pv) {
+                            const float *__restrict__ vals, const int *__restrict__ extra, int nrows, int K,
+                            int *const *__restrict__ prp, int *const *__restrict__ pci, float *const *__restrict__ pv,
+                            int *const *__restrict__ pex) {
   const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= nrows) return;
@@ -73,29 +72,129 @@ __global__ void k_part_copy(const int *__restrict__ rowptr, const int *__restric
     for (int i = lane; i < n; i += 32) {
       pci[p][d0 + i] = colind[src + i];
       if (vals) pv[p][d0 + i] = vals[src + i];
+      if (extra) pex[p][d0 + i] = extra[src + i];
     }
     src += n;
   }
 }
 
-}  // namespace gbs
-
-using namespace gbs;
-
-static void free_plan(gbs_csr_spmm_plan *P) {
-  if (!P) return;
-  if (P->owned) {
+void ColumnParts::release() {
+  if (owned) {
     int cur = 0;
     cudaGetDevice(&cur);
-    cudaSetDevice(P->device);
-    for (auto p : P->rowptr) cudaFree(p);
-    for (auto p : P->colind) cudaFree(p);
-    for (auto p : P->vals)
+    cudaSetDevice(device);
+    for (auto p : rowptr) cudaFree(p);
+    for (auto p : colind) cudaFree(p);
+    for (auto p : vals)
+      if (p) cudaFree(p);
+    for (auto p : extra)
       if (p) cudaFree(p);
     cudaSetDevice(cur);
   }
-  delete P;
+  rowptr.clear();
+  colind.clear();
+  vals.clear();
+  extra.clear();
+  nnz.clear();
+  owned = false;
+  K = 0;
 }
+
+gbs_status auto_parts(double bbytes, long long nnz, int ncols, int *K) {
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  const double half_l2 = 0.5 * (double)di.l2_bytes;
+  int k = 1;
+  if (bbytes > half_l2 && (double)nnz >= 8.0 * ncols)
+    while (k < 8 && bbytes / k > half_l2) k *= 2;
+  *K = k;
+  return GBS_OK;
+}
+
+namespace {
+template <typename T>
+gbs_status dev_alloc(T **p, size_t count) {
+  cudaError_t e = cudaMalloc(p, sizeof(T) * (count > 0 ? count : 1));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(e, "cudaMalloc");
+  }
+  return GBS_OK;
+}
+
+gbs_status partition_impl(int nrows, int ncols, int nnz, const int *rowptr, const int *colind, const float *vals,
+                          const int *extra, int K, cudaStream_t s, ColumnParts *P) {
+  const int S = (ncols + K - 1) / K;
+  DevBuf len, tables;
+  GBS_TRY(len.alloc(sizeof(int) * (size_t)K * (nrows + 1), s));
+  k_part_bounds<<<(nrows + 1 + 255) / 256, 256, 0, s>>>(rowptr, colind, nrows, K, S, len.as<int>());
+  GBS_TRY(check_launch("k_part_bounds"));
+  std::vector<int> totals(K);
+  for (int p = 0; p < K; ++p) {
+    int *rp = nullptr;
+    GBS_TRY(dev_alloc(&rp, (size_t)nrows + 1));
+    P->rowptr.push_back(rp);
+    GBS_TRY(exclusive_scan_i32(len.as<int>() + (size_t)p * (nrows + 1), rp, nrows + 1, s));
+    GBS_CUDA_TRY(cudaMemcpyAsync(&totals[p], rp + nrows, sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int p = 0; p < K; ++p) {
+    int *ci = nullptr, *ex = nullptr;
+    float *v = nullptr;
+    GBS_TRY(dev_alloc(&ci, (size_t)totals[p]));
+    P->colind.push_back(ci);
+    if (vals) GBS_TRY(dev_alloc(&v, (size_t)totals[p]));
+    P->vals.push_back(v);
+    if (extra) GBS_TRY(dev_alloc(&ex, (size_t)totals[p]));
+    P->extra.push_back(ex);
+    P->nnz.push_back(totals[p]);
+  }
+  GBS_TRY(tables.alloc(sizeof(void *) * 4 * (size_t)K, s));
+  std::vector<void *> host(4 * (size_t)K);
+  for (int p = 0; p < K; ++p) {
+    host[p] = P->rowptr[p];
+    host[K + p] = P->colind[p];
+    host[2 * K + p] = P->vals[p];
+    host[3 * K + p] = P->extra[p];
+  }
+  GBS_CUDA_TRY(cudaMemcpyAsync(tables.p, host.data(), sizeof(void *) * host.size(), cudaMemcpyHostToDevice, s));
+  void **tab = tables.as<void *>();
+  k_part_copy<<<(int)(((long long)nrows * 32 + 255) / 256), 256, 0, s>>>(
+      rowptr, colind, vals, extra, nrows, K, reinterpret_cast<int *const *>(tab),
+      reinterpret_cast<int *const *>(tab + K), reinterpret_cast<float *const *>(tab + 2 * K),
+      reinterpret_cast<int *const *>(tab + 3 * K));
+  GBS_TRY(check_launch("k_part_copy"));
+  // the host table is read by the copy above: wait before it goes out of scope
+  GBS_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBS_OK;
+}
+}  // namespace
+
+gbs_status partition_columns(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                             const float *vals, const int *extra, int K, cudaStream_t s, ColumnParts *P) {
+  P->release();
+  if (K > ncols && ncols > 0) K = ncols;
+  if (K < 1) K = 1;
+  GBS_CUDA_TRY(cudaGetDevice(&P->device));
+  P->K = K;
+  if (K == 1) {
+    P->owned = false;
+    P->rowptr.push_back(const_cast<int *>(rowptr));
+    P->colind.push_back(const_cast<int *>(colind));
+    P->vals.push_back(const_cast<float *>(vals));
+    P->extra.push_back(const_cast<int *>(extra));
+    P->nnz.push_back(nnz);
+    return GBS_OK;
+  }
+  P->owned = true;
+  gbs_status st = partition_impl(nrows, ncols, nnz, rowptr, colind, vals, extra, K, s, P);
+  if (st != GBS_OK) P->release();
+  return st;
+}
+
+}  // namespace gbs
+
+using namespace gbs;
 
 extern "C" gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
                                                const float *vals, gbs_dtype btype, int F, int parts,
@@ -106,110 +205,19 @@ extern "C" gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz, co
   GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "spmm plan: bad dtype");
   GBS_TRY(spmm_check_args(nrows, ncols, nnz, rowptr, colind, (const void *)1, F, (const float *)1));
   GBS_REQUIRE(parts >= 0 && parts <= 64, "spmm plan: parts must be 0 (auto) .. 64");
-  cudaStream_t s = (cudaStream_t)stream;
   int K = parts;
-  if (K == 0) {
-    DeviceInfo di;
-    GBS_TRY(device_info(&di));
-    const double bbytes = (double)ncols * F * (btype == GBS_F32 ? 4.0 : 2.0);
-    K = 1;
-    if (bbytes > (double)di.l2_bytes && (double)nnz >= 8.0 * ncols) {
-      while (K < 8 && bbytes / K > 0.5 * (double)di.l2_bytes) K *= 2;
-    }
-  }
-  if (K > ncols && ncols > 0) K = ncols;
-  if (K < 1) K = 1;
+  if (K == 0) GBS_TRY(auto_parts((double)ncols * F * (btype == GBS_F32 ? 4.0 : 2.0), nnz, ncols, &K));
   auto *P = new gbs_csr_spmm_plan();
   P->nrows = nrows;
   P->ncols = ncols;
   P->nnz = nnz;
   P->F = F;
-  P->K = K;
   P->btype = btype;
-  cudaGetDevice(&P->device);
-  if (K == 1) {
-    P->owned = false;
-    P->rowptr.push_back(const_cast<int *>(rowptr));
-    P->colind.push_back(const_cast<int *>(colind));
-    P->vals.push_back(const_cast<float *>(vals));
-    P->part_nnz.push_back(nnz);
-    *out = P;
-    return GBS_OK;
-  }
-  P->owned = true;
-  const int S = (ncols + K - 1) / K;
-  gbs_status st = GBS_OK;
-  {
-    DevBuf len, tables;
-    if ((st = len.alloc(sizeof(int) * (size_t)K * (nrows + 1), s)) != GBS_OK) {
-      free_plan(P);
-      return st;
-    }
-    k_part_bounds<<<(nrows + 1 + 255) / 256, 256, 0, s>>>(rowptr, colind, nrows, K, S, len.as<int>());
-    if ((st = check_launch("k_part_bounds")) != GBS_OK) {
-      free_plan(P);
-      return st;
-    }
-    std::vector<int> totals(K);
-    for (int p = 0; p < K; ++p) {
-      int *rp = nullptr;
-      cudaError_t e = cudaMalloc(&rp, sizeof(int) * ((size_t)nrows + 1));
-      if (e != cudaSuccess) {
-        free_plan(P);
-        return cuda_fail(e, "cudaMalloc");
-      }
-      P->rowptr.push_back(rp);
-      if ((st = exclusive_scan_i32(len.as<int>() + (size_t)p * (nrows + 1), rp, nrows + 1, s)) != GBS_OK) {
-        free_plan(P);
-        return st;
-      }
-      cudaMemcpyAsync(&totals[p], rp + nrows, sizeof(int), cudaMemcpyDeviceToHost, s);
-    }
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      free_plan(P);
-      return cuda_fail(e, "cudaStreamSynchronize");
-    }
-    for (int p = 0; p < K; ++p) {
-      int *ci = nullptr;
-      float *v = nullptr;
-      if ((e = cudaMalloc(&ci, sizeof(int) * (size_t)(totals[p] > 0 ? totals[p] : 1))) != cudaSuccess) {
-        free_plan(P);
-        return cuda_fail(e, "cudaMalloc");
-      }
-      P->colind.push_back(ci);
-      if (vals) {
-        if ((e = cudaMalloc(&v, sizeof(float) * (size_t)(totals[p] > 0 ? totals[p] : 1))) != cudaSuccess) {
-          free_plan(P);
-          return cuda_fail(e, "cudaMalloc");
-        }
-      }
-      P->vals.push_back(v);
-      P->part_nnz.push_back(totals[p]);
-    }
-    if ((st = tables.alloc(sizeof(void *) * 3 * (size_t)K, s)) != GBS_OK) {
-      free_plan(P);
-      return st;
-    }
-    std::vector<void *> host(3 * (size_t)K);
-    for (int p = 0; p < K; ++p) {
-      host[p] = P->rowptr[p];
-      host[K + p] = P->colind[p];
-      host[2 * K + p] = P->vals[p];
-    }
-    cudaMemcpyAsync(tables.p, host.data(), sizeof(void *) * host.size(), cudaMemcpyHostToDevice, s);
-    void **tab = tables.as<void *>();
-    k_part_copy<<<(int)(((long long)nrows * 32 + 255) / 256), 256, 0, s>>>(
-        rowptr, colind, vals, nrows, K, reinterpret_cast<int *const *>(tab), reinterpret_cast<int *const *>(tab + K),
-        reinterpret_cast<float *const *>(tab + 2 * K));
-    if ((st = check_launch("k_part_copy")) != GBS_OK) {
-      free_plan(P);
-      return st;
-    }
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
-      free_plan(P);
-      return cuda_fail(e, "cudaStreamSynchronize");
-    }
+  gbs_status st = partition_columns(nrows, ncols, nnz, rowptr, colind, vals, nullptr, K, (cudaStream_t)stream,
+                                    &P->parts);
+  if (st != GBS_OK) {
+    delete P;
+    return st;
   }
   *out = P;
   return GBS_OK;
@@ -218,13 +226,16 @@ extern "C" gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz, co
 extern "C" gbs_status gbs_csr_spmm_plan_parts(const gbs_csr_spmm_plan *P, int *parts) {
   clear_error();
   GBS_REQUIRE(P && parts, "spmm plan: null argument");
-  *parts = P->K;
+  *parts = P->parts.K;
   return GBS_OK;
 }
 
 extern "C" gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *P) {
   clear_error();
-  free_plan(P);
+  if (P) {
+    P->parts.release();
+    delete P;
+  }
   return GBS_OK;
 }
 
@@ -235,11 +246,12 @@ extern "C" gbs_status gbs_csr_spmm_planned(const gbs_csr_spmm_plan *P, const voi
   if (P->nrows == 0) return GBS_OK;
   GBS_REQUIRE(B && C, "spmm planned: null B or C");
   const int dt = P->btype == GBS_F32 ? 0 : (P->btype == GBS_BF16 ? 1 : 2);
-  for (int p = 0; p < P->K; ++p) {
+  const ColumnParts &cp = P->parts;
+  for (int p = 0; p < cp.K; ++p) {
     SpmmPlan sp;
-    GBS_TRY(spmm_plan(dt, P->nrows, P->ncols, P->part_nnz[p], P->F, B, C, 0, &sp));
+    GBS_TRY(spmm_plan(dt, P->nrows, P->ncols, cp.nnz[p], P->F, B, C, 0, &sp, (P->ncols + cp.K - 1) / cp.K));
     GBS_REQUIRE(ws != nullptr && ws_bytes >= sp.ws_bytes, "spmm planned: workspace missing or too small");
-    GBS_TRY(spmm_run(sp, P->nrows, P->part_nnz[p], P->rowptr[p], P->colind[p], P->vals[p], B, P->F, C, ws,
+    GBS_TRY(spmm_run(sp, P->nrows, cp.nnz[p], cp.rowptr[p], cp.colind[p], cp.vals[p], B, P->F, C, ws,
                      (cudaStream_t)stream, 0, p > 0 ? 1 : 0));
   }
   return GBS_OK;

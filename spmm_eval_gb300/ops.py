@@ -420,6 +420,52 @@ def spmm_backward(T: "CSRTranspose", t_vals: torch.Tensor | None, dC: torch.Tens
     return dB, dvals
 
 
+class BackwardPlan:
+    """Planned fused backward (gbs_spmm_backward_plan_*): A^T split by row
+    ranges of A so that each pass's dC gathers stay in L2 (parts = 0: the
+    library chooses from dC's size against L2).  t_vals is copied at
+    creation; with one part the plan keeps references to T and t_vals."""
+
+    def __init__(self, T: "CSRTranspose", t_vals: torch.Tensor | None, F: int,
+                 dtype: torch.dtype = torch.float32, parts: int = 0):
+        if t_vals is not None:
+            _check_cuda("t_vals", t_vals, torch.float32)
+        self.T, self.t_vals, self.F, self.dtype = T, t_vals, F, dtype
+        h = C.c_void_p()
+        _lib.call("gbs_spmm_backward_plan_create", T._h, _ptr(t_vals), _DT[dtype], F, parts,
+                  _stream(T.device), C.byref(h))
+        self._h = h
+        k = C.c_int(0)
+        _lib.call("gbs_spmm_backward_plan_parts", h, C.byref(k))
+        self.parts = int(k.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbs_spmm_backward_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self, dC: torch.Tensor, H: torch.Tensor, dB: torch.Tensor | None = None,
+            dvals: torch.Tensor | None = None, workspace: SpmmWorkspace | None = None):
+        _check_cuda("dC", dC, self.dtype)
+        _check_cuda("H", H, self.dtype)
+        T = self.T
+        if tuple(dC.shape) != (T.nrows, self.F) or tuple(H.shape) != (T.ncols, self.F):
+            raise ValueError("dC / H do not match the plan")
+        if dB is None:
+            dB = torch.empty((T.ncols, self.F), dtype=torch.float32, device=dC.device)
+        if dvals is None:
+            dvals = torch.empty(T.nnz, dtype=torch.float32, device=dC.device)
+        ws = workspace or SpmmWorkspace()
+        buf = ws.get(spmm_workspace_bytes(T.ncols, T.nnz, self.F, self.dtype), dC.device)
+        _lib.call("gbs_spmm_backward_planned", self._h, _ptr(dC), _ptr(H), _ptr(dB), _ptr(dvals), _ptr(buf),
+                  buf.numel(), _stream(dC.device))
+        return dB, dvals
+
+
 def sddmm(A: CSR, G: torch.Tensor, H: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """out[e] = <G[row(e)], H[col(e)]> on A's pattern (FP32)."""
     A.validate_layout()

@@ -195,3 +195,53 @@ def test_fused_backward_matches_separate(cuda, dtype, F):
     refv = oracle.sddmm_f64(rp, ci, Gr, Hr)
     S = sddmm_scale(rp, ci, Gr, Hr)
     assert np.max(np.abs(dv.cpu().numpy() - refv) / np.maximum(S, 1e-30)) <= 1e-5
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("parts", [1, 2, 3, 4])
+def test_planned_backward(cuda, dtype, parts):
+    """gbs_spmm_backward_planned (A^T split by row ranges of A, accumulating
+    dB passes) against FP64 oracles of both outputs and against the one-pass
+    fused backward."""
+    g = G.gcn_normalize(G.flickr_like())
+    n, F = g.nrows, 64
+    Gm = G.normal(F, 23, (n, F))
+    Hm = G.normal(F, 24, (n, F))
+    Gd, Hd = Gm.to(dtype).to(cuda), Hm.to(dtype).to(cuda)
+    T = ops.CSRTranspose(dev(g, cuda, False))
+    tv = T.values(g.vals.to(cuda))
+    plan = ops.BackwardPlan(T, tv, F, dtype, parts)
+    assert plan.parts == parts
+    dB, dv = plan.run(Gd, Hd)
+    dB1, dv1 = ops.spmm_backward(T, tv, Gd, Hd)
+    rp, ci, v = g.rowptr.numpy(), g.colind.numpy(), g.vals.numpy()
+    Gr, Hr = Gd.float().cpu().numpy(), Hd.float().cpu().numpy()
+    wrp, wci, wpm = oracle.csr_transpose(n, n, rp, ci)
+    ref, mag = oracle.csr_spmm_f64(wrp, wci, v[wpm], Gr)
+    assert oracle.rel_err(dB.cpu().numpy(), ref, mag)[0] <= 1e-5
+    refv = oracle.sddmm_f64(rp, ci, Gr, Hr)
+    S = sddmm_scale(rp, ci, Gr, Hr)
+    assert np.max(np.abs(dv.cpu().numpy() - refv) / np.maximum(S, 1e-30)) <= 1e-5
+    assert torch.allclose(dB, dB1, rtol=1e-5, atol=1e-6)
+    assert torch.allclose(dv, dv1, rtol=1e-5, atol=1e-6)
+    if parts == 1:
+        assert torch.equal(dB, dB1) and torch.equal(dv, dv1)
+
+
+def test_planned_backward_auto_parts_and_reuse(cuda):
+    """Automatic part count (1 when dC fits in half of L2) and a plan reused
+    across calls with a shared workspace."""
+    g = G.gcn_normalize(G.flickr_like())
+    n, F = g.nrows, 32
+    T = ops.CSRTranspose(dev(g, cuda, False))
+    tv = T.values(g.vals.to(cuda))
+    plan = ops.BackwardPlan(T, tv, F, torch.float32, 0)
+    assert plan.parts == 1
+    ws = ops.SpmmWorkspace()
+    outs = []
+    for seed in (1, 2):
+        Gd = G.normal(seed, 30, (n, F)).to(cuda)
+        Hd = G.normal(seed, 31, (n, F)).to(cuda)
+        outs.append((plan.run(Gd, Hd, workspace=ws), ops.spmm_backward(T, tv, Gd, Hd, workspace=ws)))
+    for (a, b) in outs:
+        assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
