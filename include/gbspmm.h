@@ -226,7 +226,9 @@ GBS_API gbs_status gbs_spmm_backward_plan_parts(const gbs_spmm_backward_plan *pl
 GBS_API gbs_status gbs_spmm_backward_plan_destroy(gbs_spmm_backward_plan *plan);
 /* Same results as gbs_spmm_backward (dB to FP32 rounding of a different
  * summation split, dvals bitwise when the dot products' lane order is
- * unchanged); workspace as gbs_spmm_backward. */
+ * unchanged); workspace as gbs_spmm_backward.  The passes write dvals in
+ * their own entry order to nnz * 4 bytes of temporaries (library pool,
+ * stream-ordered) and a final gather puts them in A's order. */
 GBS_API gbs_status gbs_spmm_backward_planned(const gbs_spmm_backward_plan *plan,
                                      const void *d_dC, const void *d_H,
                                      float *d_dB, float *d_dvals,

@@ -20,6 +20,15 @@ __device__ __forceinline__ void fma2(float &acc0, float &acc1, float v, float x0
       : "f"(v), "f"(x0), "f"(x1));
 }
 
+// (acc0, acc1) += (a0 * b0, a1 * b1) as one FFMA2: two interleaved partial
+// sums of a dot product.
+__device__ __forceinline__ void fma2v(float &acc0, float &acc1, float a0, float a1, float b0, float b1) {
+  asm("{\n .reg .b64 aa, bb, cc;\n mov.b64 aa, {%2, %3};\n mov.b64 bb, {%4, %5};\n"
+      " mov.b64 cc, {%0, %1};\n fma.rn.f32x2 cc, aa, bb, cc;\n mov.b64 {%0, %1}, cc;\n}"
+      : "+f"(acc0), "+f"(acc1)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 template <int DT, int VEC>
 struct Feat;
 

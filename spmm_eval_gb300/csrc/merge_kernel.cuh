@@ -47,7 +47,7 @@ struct MergeArgs {
   int accumulate;  // 1: C += A B (C read, added, written); 0: C = A B
   // fused SDDMM (SD kernels only)
   const void *H;     // rows indexed like C, F elements, B's type
-  float *dvals;      // output, indexed through perm
+  float *dvals;      // output, indexed through perm (or by entry when perm is null)
   const int *perm;   // entry e of this matrix -> index in dvals
 };
 
@@ -134,17 +134,25 @@ struct MergeKernel {
   // a multi-value butterfly ((U - 1) + log2(LPR / U) shuffles per U entries).
   static __device__ __forceinline__ void sddmm_round(const MergeArgs &a, int base, int u0, int n_valid, int sub,
                                                      int sl, const float (&h)[CH][VEC], const raw (&bv)[U][CH]) {
+    // per entry: even and odd columns summed as the two halves of FFMA2s,
+    // then added
     float s[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      s[u] = 0.f;
+      float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         float x[VEC];
         F_::widen(x, bv[u][c]);
+        if constexpr (VEC % 2 == 0) {
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) s[u] = fmaf(h[c][q], x[q], s[u]);
+          for (int q = 0; q < VEC; q += 2) fma2v(s0, s1, h[c][q], h[c][q + 1], x[q], x[q + 1]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) s0 = fmaf(h[c][q], x[q], s0);
+        }
       }
+      s[u] = s0 + s1;
     }
     int nv = U;
 #pragma unroll
@@ -167,7 +175,10 @@ struct MergeKernel {
     }
     const int span = LPR / U;
     const int k = (u0 + sl / span) * NSUB + sub;
-    if (sl % span == 0 && k < n_valid) a.dvals[__ldg(a.perm + a.rp_base + base + k)] = s[0];
+    if (sl % span == 0 && k < n_valid) {
+      const long long e = (long long)a.rp_base + base + k;
+      a.dvals[a.perm ? (long long)__ldg(a.perm + e) : e] = s[0];
+    }
   }
 
   // H row r (this lane's chunks), widened to FP32.
