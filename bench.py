@@ -50,12 +50,13 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the SpMM kernel from the committed ncu
-    summary (None until one exists)."""
-    p = ROOT / "profiles" / "csr_spmm_reddit_f256.json"
+    """DRAM bytes of one bench step (the planned SpMM's accumulating
+    launches together) from the committed ncu summary (None until one
+    exists)."""
+    p = ROOT / "profiles" / "csr_spmm_plan_reddit_f256.json"
     if p.exists():
         try:
-            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+            return json.loads(p.read_text()).get("dram_bytes_per_step")
         except Exception:
             return None
     return None
@@ -396,8 +397,10 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "peak_source": peak_kind,
-                     "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per launch",
-                     "bytes_per_launch": bytes_f32},
+                     "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per SpMM",
+                     "bytes_per_step": bytes_f32,
+                     "per": "step = one SpMM = %d accumulating launches of k_csr_spmm_merge "
+                            "(achieved and traffic both per step)" % plan32.parts},
         "fwd_bwd": {"what": "planned SpMM A H + planned fused backward (A^T dY and SDDMM(dY, H) in one pass "
                             "per row-range piece of A^T), F=256",
                     "backward_parts": {"f32": bplans[torch.float32].parts, "bf16": bplans[torch.bfloat16].parts},

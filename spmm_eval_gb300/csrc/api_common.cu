@@ -64,6 +64,18 @@ gbs_status lib_pool(cudaMemPool_t *out) {
   return GBS_OK;
 }
 
+gbs_status side_stream(cudaStream_t *out) {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "device ordinal >= 64");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!streams[dev]) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+  *out = streams[dev];
+  return GBS_OK;
+}
+
 }  // namespace gbs
 
 extern "C" gbs_status gbs_pool_trim(void) {

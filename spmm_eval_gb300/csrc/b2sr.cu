@@ -165,6 +165,12 @@ struct B2srSpmmArgs {
   int nvec;
   long long ldb, ldc;
   float *C;
+  // Hub split.  The main pass leaves block-rows of more than hub_min tiles
+  // (0: none) to the hub pass, which reads hubs = [count, block-row ids ...]
+  // and covers each hub's feature chunks in `slices` slices.
+  int hub_min;
+  const int *hubs;
+  int slices;
 };
 
 template <int TS>
@@ -173,24 +179,31 @@ __device__ __forceinline__ uint32_t tile_row(const void *val, size_t t, int r) {
   return (uint32_t)__ldg(reinterpret_cast<const VT *>(val) + t * TS + r);
 }
 
-template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ>
-__global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
+// One warp: block-row br, tile rows [grp * R, grp * R + R), feature chunks
+// chunk0 + [0, LPR * CH); U entries gathered per round.  The tiles are read
+// G groups (of 32 / TS tiles = 32 entries) at a time; the entries of a step
+// that touch the warp's rows are compacted, in order, into a per-warp list in
+// shared memory (ballot + prefix popcount), and the gathers then run over the
+// list U at a time while the next step's indices and tile rows are loaded.
+// Entries are added in group order and, inside a group, in lane order, so
+// every output element is the same sequence of FP32 additions as a
+// one-group-at-a-time walk.  `list` holds 32 * G entries (col, row bits).
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G>
+__device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long br, int grp, int chunk0,
+                                               int lane, int2 *list) {
   constexpr int NSUB = 32 / LPR;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;  // tile rows per warp
-  constexpr int NG = (TS + R - 1) / R;                  // row groups per block-row
   constexpr int TPG = 32 / TS;                          // tiles per 32 entries
+  constexpr int TPS = TPG * G;                          // tiles per step
   constexpr bool REF_ORDER = (TS == 4);
-  constexpr int U = 4;
   using F_ = Feat<DT, VEC>;
   using raw = typename F_::raw;
 
-  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long br = gw / NG;
-  if (br >= a.mb) return;
-  const int row0 = (int)(gw % NG) * R;
+  const int sub = lane / LPR, sl = lane % LPR;
+  const int row0 = grp * R;
   const int my0 = sub * RPS;  // my first row inside the warp's group
   const unsigned my_mask = ((1u << RPS) - 1u) << my0;
+  const unsigned lt_mask = (1u << lane) - 1u;
 
   float acc[RPS][CH][VEC];
 #pragma unroll
@@ -203,33 +216,47 @@ __global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
   const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
   const int j = REF_ORDER ? lane / TPG : lane % TS;
   const int l = REF_ORDER ? lane % TPG : lane / TS;
-  for (int g0 = tb; g0 < te; g0 += TPG) {
-    const int t = g0 + l;
-    unsigned rmask = 0;
-    int brow = 0;
-    if (t < te) {
-      brow = __ldg(a.colind + t) * TS + j;
+  // this lane's entry (feature row, row bits) in each of G groups
+  int nb[G];
+  unsigned nm[G];
+  auto load_step = [&](int s0) {
 #pragma unroll
-      for (int i = 0; i < R; ++i)
-        if (row0 + i < TS) rmask |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+    for (int g = 0; g < G; ++g) {
+      const int t = s0 + g * TPG + l;
+      nb[g] = 0;
+      nm[g] = 0;
+      if (t < te) {
+        nb[g] = __ldg(a.colind + t) * TS + j;
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+          if (row0 + i < TS) nm[g] |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+      }
     }
-    unsigned act = __ballot_sync(0xffffffffu, rmask != 0);
-    while (act) {
+  };
+  if (tb < te) load_step(tb);
+  for (int s0 = tb; s0 < te; s0 += TPS) {
+    int n = 0;
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const unsigned act = __ballot_sync(0xffffffffu, nm[g] != 0);
+      if (nm[g] != 0) list[n + __popc(act & lt_mask)] = make_int2(nb[g], (int)nm[g]);
+      n += __popc(act);
+    }
+    __syncwarp();
+    if (s0 + TPS < te) load_step(s0 + TPS);  // next step's indices, in flight during the gathers
+    for (int k0 = 0; k0 < n; k0 += U) {
       raw bv[U][CH];
       unsigned mu[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int e = act ? __ffs(act) - 1 : 0;
-        const bool live = act != 0;
-        act &= act - 1;
-        const int col = __shfl_sync(0xffffffffu, brow, e);
-        const unsigned m = __shfl_sync(0xffffffffu, rmask, e);
-        mu[u] = live ? m : 0u;
+        const bool live = k0 + u < n;
+        const int2 en = live ? list[k0 + u] : make_int2(0, 0);
+        mu[u] = (unsigned)en.y;
         const bool need = (mu[u] & my_mask) != 0;
-        const size_t rb = (size_t)col * (size_t)a.ldb;
+        const size_t rb = (size_t)en.x * (size_t)a.ldb;
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
-          const int chunk = c * LPR + sl;
+          const int chunk = chunk0 + c * LPR + sl;
           if (need && chunk < a.nvec) bv[u][c] = F_::load(a.B, rb + (size_t)chunk * VEC);
           else bv[u][c] = F_::zero();
         }
@@ -248,6 +275,7 @@ __global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
         }
       }
     }
+    __syncwarp();  // the list is rewritten by the next step
   }
 #pragma unroll
   for (int k = 0; k < RPS; ++k) {
@@ -258,7 +286,7 @@ __global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
     float *dst = a.C + (size_t)orow * a.ldc;
 #pragma unroll
     for (int c = 0; c < CH; ++c) {
-      const int chunk = c * LPR + sl;
+      const int chunk = chunk0 + c * LPR + sl;
       if (chunk >= a.nvec) continue;
       if (STORE_NZ) {
 #pragma unroll
@@ -271,11 +299,67 @@ __global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
   }
 }
 
+// Main pass: one warp per (block-row, group of R tile rows), all features,
+// 4 entries per round.
+constexpr int MAIN_G = 2;
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ>
+__global__ void __launch_bounds__(256) k_b2sr_spmm(B2srSpmmArgs a) {
+  constexpr int NSUB = 32 / LPR;
+  constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
+  constexpr int NG = (TS + R - 1) / R;
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long br = gw / NG;
+  if (br >= a.mb) return;
+  if (a.hub_min > 0 && __ldg(a.rowptr + br + 1) - __ldg(a.rowptr + br) > a.hub_min) return;
+  __shared__ int2 lists[8][32 * MAIN_G];
+  b2sr_block_row<TS, DT, VEC, LPR, CH, RPS, STORE_NZ, 4, MAIN_G>(a, br, (int)(gw % NG), 0, lane,
+                                                                 lists[threadIdx.x >> 5]);
+}
+
+// Hub pass: the block-rows a single warp would walk for far longer than any
+// other (power-law hubs: thousands of tiles against a mean of tens).  The
+// order of additions into an output element has to stay the tile walk's,
+// so a hub is not split along its tiles.  Instead a hub is split by tile row
+// and by feature slices of 32 16-byte chunks: one warp walks the tiles for
+// one row and one slice, so every entry it keeps is a gather all 32 lanes
+// use, and with one row per warp the registers allow HUB_U = 16 gathers per
+// round instead of 4 -- the warp's chain of dependent memory round trips is
+// what bounds a hub, not bandwidth.  Work items (hub, row, slice) are taken
+// grid-stride.
+constexpr int HUB_CHUNKS = 32;
+constexpr int HUB_U = 16;
+template <int TS, int DT, int VEC, bool STORE_NZ>
+__global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hubs(B2srSpmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long items = (long long)__ldg(a.hubs) * TS * a.slices;
+  __shared__ int2 lists[8][32 * 4];
+  for (long long it = gw; it < items; it += nw) {
+    const int sl = (int)(it % a.slices);
+    const long long rest = it / a.slices;
+    const int row = (int)(rest % TS);
+    const long long br = __ldg(a.hubs + 1 + rest / TS);
+    b2sr_block_row<TS, DT, VEC, 32, 1, 1, STORE_NZ, HUB_U, 4>(a, br, row, sl * HUB_CHUNKS, lane,
+                                                              lists[threadIdx.x >> 5]);
+  }
+}
+
+// hubs[0] = number of block-rows with more than hub_min tiles, hubs[1..] =
+// their ids (any order: each output element is computed whole by one warp).
+__global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs) {
+  const int br = blockIdx.x * blockDim.x + threadIdx.x;
+  if (br >= mb) return;
+  if (rowptr[br + 1] - rowptr[br] > hub_min) hubs[1 + atomicAdd(hubs, 1)] = br;
+}
+
 namespace {
 
 struct B2srVariant {
   const void *fn;
   int vec, lpr, ch, rows_per_warp, groups;
+  const void *hub_fn;  // hub pass (32-chunk slices), same tile size and type
 };
 
 template <int TS, int DT, int VEC, int LPR, int CH, bool NZ>
@@ -286,7 +370,7 @@ B2srVariant mk_b2sr() {
   constexpr int RPS = (NSUB * RPS1 > TS) ? ((TS / NSUB) > 0 ? TS / NSUB : 1) : RPS1;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
   return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
-                     (TS + R - 1) / R};
+                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>};
 }
 
 template <int TS, int DT, int VEC, bool NZ>
@@ -315,6 +399,25 @@ bool pick_ts(int dt, int F, bool vec16, B2srVariant *v) {
 }
 
 bool is_aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Block-rows of more tiles than this go to the hub pass (the mean of a
+// power-law graph's tile-4 block-rows is ~40; its largest hubs have
+// thousands); matrices of fewer block-rows run in one pass.
+constexpr int kHubTiles = 256;
+constexpr int kHubMinBlockRows = 1024;
+
+// Per-call events (created and destroyed around one fork/join).
+struct Events {
+  cudaEvent_t e[2] = {nullptr, nullptr};
+  int n = 0;
+  gbs_status create(int k) {
+    for (n = 0; n < k; ++n) GBS_CUDA_TRY(cudaEventCreateWithFlags(&e[n], cudaEventDisableTiming));
+    return GBS_OK;
+  }
+  ~Events() {
+    for (int i = 0; i < n; ++i) cudaEventDestroy(e[i]);
+  }
+};
 
 }  // namespace
 
@@ -346,11 +449,46 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
   a.ldb = F;
   a.ldc = F;
   a.C = C;
+  a.hub_min = 0;
+  a.hubs = nullptr;
+  a.slices = (a.nvec + HUB_CHUNKS - 1) / HUB_CHUNKS;
   const long long warps = (long long)mb * v.groups;
   const int blocks = (int)((warps * 32 + 255) / 256);
+  if (mb < kHubMinBlockRows) {
+    void *args[] = {&a};
+    GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s));
+    return GBS_OK;
+  }
+  // Hub block-rows go to a concurrent pass on a side stream:
+  //   s: find hubs -> fork -> main pass (hubs skipped) -> join
+  //   side:                -> hub pass ---------------/
+  DevBuf hubs;
+  GBS_TRY(hubs.alloc(sizeof(int) * ((size_t)mb + 1), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(hubs.p, 0, sizeof(int), s));
+  k_find_hubs<<<(mb + 255) / 256, 256, 0, s>>>(rowptr, mb, kHubTiles, hubs.as<int>());
+  GBS_TRY(check_launch("k_find_hubs"));
+  a.hub_min = kHubTiles;
+  a.hubs = hubs.as<int>();
+  cudaStream_t side = nullptr;
+  GBS_TRY(side_stream(&side));
+  Events ev;
+  GBS_TRY(ev.create(2));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
   void *args[] = {&a};
-  GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s));
-  return GBS_OK;
+  // enough warps that every (hub, group, slice) item of a typical graph gets
+  // its own warp (surplus warps exit at once)
+  GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
+  gbs_status st = GBS_OK;
+  cudaError_t e = cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s);
+  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_spmm");
+  // join even on failure, so the side stream's work is ordered before
+  // anything the caller enqueues next (and before the list is freed)
+  GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[1], 0));
+  return st;
 }
 
 // ---------------------------------------------------------------------------

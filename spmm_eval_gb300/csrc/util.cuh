@@ -25,6 +25,9 @@ inline int bits_for(long long v) {
 // synchronisation).  gbs_pool_trim releases what it keeps.
 constexpr unsigned long long kPoolKeepBytes = 8ull << 30;
 gbs_status lib_pool(cudaMemPool_t *out);
+// A non-blocking stream per device for a sub-pass that runs beside the
+// caller's stream (forked and joined with events inside one call).
+gbs_status side_stream(cudaStream_t *out);
 
 // RAII device buffer from stream-ordered allocation in the library pool
 // (freed on the same stream).  Used only where an entry point documents that

@@ -188,6 +188,21 @@ def test_b2sr_spmm_exact_on_binary_features(cuda, ts, F):
 
 
 @pytest.mark.parametrize("ts", TILES)
+@pytest.mark.parametrize("F", [64, 512])
+def test_b2sr_spmm_bf16_features_hub_split(cuda, ts, F):
+    """16-bit features through both passes (block-rows of more than 256 tiles
+    go to the sliced hub pass): +-1 values, so the result equals the FP32
+    CSR product exactly."""
+    g = G.flickr_like()
+    A = ops.CSR(g.rowptr.to(cuda), g.colind.to(cuda), None, g.nrows, g.ncols)
+    Ab = ops.csr2b2sr(A, ts)
+    rng = np.random.default_rng(7 * ts + F)
+    Bpm = torch.from_numpy(rng.integers(0, 2, (g.ncols, F)).astype(np.float32) * 2 - 1).to(cuda)
+    got = ops.b2sr_spmm(Ab, Bpm.to(torch.bfloat16))
+    assert torch.equal(got, ops.csr_spmm(A, Bpm))
+
+
+@pytest.mark.parametrize("ts", TILES)
 def test_b2sr_spmm_float_features_vs_oracle(cuda, ts):
     name, n, m, rp, ci = GRAPHS[4]
     brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
