@@ -507,19 +507,20 @@ struct B2srBmmArgs {
   const uint32_t *X;
   int32_t *C;
   int signed_form;
+  int hub_min;      // main pass: leave block-rows of more tiles to the hub pass (0: none)
+  const int *hubs;  // hub pass: [count, block-row ids ...]
 };
 
-template <int TS, int WMAX>
-__global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
-  constexpr int R0 = 32 / WMAX > 0 ? 32 / WMAX : 1;
-  constexpr int R = R0 < TS ? R0 : TS;
-  constexpr int NG = (TS + R - 1) / R;
+// One warp: block-row br, tile rows [grp * R, grp * R + R).  Entries of G
+// groups at a time are compacted into the per-warp shared-memory list (as
+// in b2sr_block_row), then gathered U at a time while the next step's
+// indices load.  Integer counts: the order of entries does not matter here.
+template <int TS, int WMAX, int R, int U, int G>
+__device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br, int grp, int lane, int2 *list) {
   constexpr int TPG = 32 / TS;
-  const int lane = threadIdx.x & 31;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long br = gw / NG;
-  if (br >= a.mb) return;
-  const int row0 = (int)(gw % NG) * R;
+  constexpr int TPS = TPG * G;
+  const int row0 = grp * R;
+  const unsigned lt_mask = (1u << lane) - 1u;
   int cnt[R][WMAX];
   int deg[R];
 #pragma unroll
@@ -531,34 +532,56 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
   const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
   const int j = lane % TS, l = lane / TS;
   const int shift = 31 - lane;
-  for (int g0 = tb; g0 < te; g0 += TPG) {
-    const int t = g0 + l;
-    unsigned rmask = 0;
-    int brow = 0;
-    if (t < te) {
-      brow = __ldg(a.colind + t) * TS + j;
+  int nb[G];
+  unsigned nm[G];
+  auto load_step = [&](int s0) {
 #pragma unroll
-      for (int i = 0; i < R; ++i)
-        if (row0 + i < TS) rmask |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+    for (int g = 0; g < G; ++g) {
+      const int t = s0 + g * TPG + l;
+      nb[g] = 0;
+      nm[g] = 0;
+      if (t < te) {
+        nb[g] = __ldg(a.colind + t) * TS + j;
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+          if (row0 + i < TS) nm[g] |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+      }
     }
-    unsigned act = __ballot_sync(0xffffffffu, rmask != 0);
-    while (act) {
-      const int e = __ffs(act) - 1;
-      act &= act - 1;
-      const int col = __shfl_sync(0xffffffffu, brow, e);
-      const unsigned m = __shfl_sync(0xffffffffu, rmask, e);
-      const uint32_t *xr = a.X + (size_t)col * a.W;
-      uint32_t w[WMAX];
+  };
+  if (tb < te) load_step(tb);
+  for (int s0 = tb; s0 < te; s0 += TPS) {
+    int n = 0;
 #pragma unroll
-      for (int k = 0; k < WMAX; ++k) w[k] = k < a.W ? __ldg(xr + k) : 0u;
-#pragma unroll
-      for (int i = 0; i < R; ++i)
-        if ((m >> i) & 1u) {
-          ++deg[i];
-#pragma unroll
-          for (int k = 0; k < WMAX; ++k) cnt[i][k] += (int)((w[k] >> shift) & 1u);
-        }
+    for (int g = 0; g < G; ++g) {
+      const unsigned act = __ballot_sync(0xffffffffu, nm[g] != 0);
+      if (nm[g] != 0) list[n + __popc(act & lt_mask)] = make_int2(nb[g], (int)nm[g]);
+      n += __popc(act);
     }
+    __syncwarp();
+    if (s0 + TPS < te) load_step(s0 + TPS);
+    for (int k0 = 0; k0 < n; k0 += U) {
+      uint32_t w[U][WMAX];
+      unsigned mu[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const bool live = k0 + u < n;
+        const int2 en = live ? list[k0 + u] : make_int2(0, 0);
+        mu[u] = (unsigned)en.y;
+        const uint32_t *xr = a.X + (size_t)en.x * a.W;
+#pragma unroll
+        for (int k = 0; k < WMAX; ++k) w[u][k] = (live && k < a.W) ? __ldg(xr + k) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+          if ((mu[u] >> i) & 1u) {
+            ++deg[i];
+#pragma unroll
+            for (int k = 0; k < WMAX; ++k) cnt[i][k] += (int)((w[u][k] >> shift) & 1u);
+          }
+    }
+    __syncwarp();
   }
 #pragma unroll
   for (int i = 0; i < R; ++i) {
@@ -575,26 +598,96 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
   }
 }
 
+template <int WMAX>
+struct BmmShape {
+  static constexpr int R0 = 32 / WMAX > 0 ? 32 / WMAX : 1;
+  static constexpr int U = 32 / WMAX > 8 ? 8 : (32 / WMAX > 0 ? 32 / WMAX : 1);  // words in flight
+};
+
+// Main pass: one warp per (block-row, group of R rows), R * WMAX <= 32
+// counters per lane.
+template <int TS, int WMAX>
+__global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
+  constexpr int R = BmmShape<WMAX>::R0 < TS ? BmmShape<WMAX>::R0 : TS;
+  constexpr int NG = (TS + R - 1) / R;
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long br = gw / NG;
+  if (br >= a.mb) return;
+  if (a.hub_min > 0 && __ldg(a.rowptr + br + 1) - __ldg(a.rowptr + br) > a.hub_min) return;
+  __shared__ int2 lists[8][32 * 2];
+  bmm_block_row<TS, WMAX, R, BmmShape<WMAX>::U, 2>(a, br, (int)(gw % NG), lane, lists[threadIdx.x >> 5]);
+}
+
+// Hub pass: one warp per (hub block-row, tile row), items grid-stride.
+template <int TS, int WMAX>
+__global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long items = (long long)__ldg(a.hubs) * TS;
+  __shared__ int2 lists[8][32 * 4];
+  for (long long it = gw; it < items; it += nw) {
+    const long long br = __ldg(a.hubs + 1 + it / TS);
+    bmm_block_row<TS, WMAX, 1, 2 * BmmShape<WMAX>::U, 4>(a, br, (int)(it % TS), lane, lists[threadIdx.x >> 5]);
+  }
+}
+
 template <int TS>
 gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
-  const void *fn = nullptr;
+  const void *fn = nullptr, *hub_fn = nullptr;
   int wmax = 0;
-  if (a.W <= 1) { fn = (const void *)&k_b2sr_bmm<TS, 1>; wmax = 1; }
-  else if (a.W <= 2) { fn = (const void *)&k_b2sr_bmm<TS, 2>; wmax = 2; }
-  else if (a.W <= 4) { fn = (const void *)&k_b2sr_bmm<TS, 4>; wmax = 4; }
-  else if (a.W <= 8) { fn = (const void *)&k_b2sr_bmm<TS, 8>; wmax = 8; }
-  else if (a.W <= 16) { fn = (const void *)&k_b2sr_bmm<TS, 16>; wmax = 16; }
-  else if (a.W <= 32) { fn = (const void *)&k_b2sr_bmm<TS, 32>; wmax = 32; }
+#define GBS_BMM_CASE(WM)                                 \
+  {                                                      \
+    fn = (const void *)&k_b2sr_bmm<TS, WM>;              \
+    hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM>;     \
+    wmax = WM;                                           \
+  }
+  if (a.W <= 1) GBS_BMM_CASE(1)
+  else if (a.W <= 2) GBS_BMM_CASE(2)
+  else if (a.W <= 4) GBS_BMM_CASE(4)
+  else if (a.W <= 8) GBS_BMM_CASE(8)
+  else if (a.W <= 16) GBS_BMM_CASE(16)
+  else if (a.W <= 32) GBS_BMM_CASE(32)
   else return fail(GBS_ERR_UNSUPPORTED, "b2sr bmm: F must be <= 1024");
+#undef GBS_BMM_CASE
   const int R0 = 32 / wmax > 0 ? 32 / wmax : 1;
   const int R = R0 < TS ? R0 : TS;
   const int NG = (TS + R - 1) / R;
   const long long warps = (long long)a.mb * NG;
   const int blocks = (int)((warps * 32 + 255) / 256);
   if (blocks == 0) return GBS_OK;
+  a.hub_min = 0;
+  a.hubs = nullptr;
+  if (a.mb < kHubMinBlockRows) {
+    void *args[] = {&a};
+    GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s));
+    return GBS_OK;
+  }
+  // main pass on s, hub pass on the side stream (as in b2sr_spmm_run)
+  DevBuf hubs;
+  GBS_TRY(hubs.alloc(sizeof(int) * ((size_t)a.mb + 1), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(hubs.p, 0, sizeof(int), s));
+  k_find_hubs<<<(a.mb + 255) / 256, 256, 0, s>>>(a.rowptr, a.mb, kHubTiles, hubs.as<int>());
+  GBS_TRY(check_launch("k_find_hubs"));
+  a.hub_min = kHubTiles;
+  a.hubs = hubs.as<int>();
+  cudaStream_t side = nullptr;
+  GBS_TRY(side_stream(&side));
+  Events ev;
+  GBS_TRY(ev.create(2));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
   void *args[] = {&a};
-  GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s));
-  return GBS_OK;
+  GBS_CUDA_TRY(cudaLaunchKernel(hub_fn, dim3(di.sm_count * 4), dim3(256), args, 0, side));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
+  gbs_status st = GBS_OK;
+  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s);
+  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_bmm");
+  GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[1], 0));
+  return st;
 }
 
 // ---------------------------------------------------------------------------
