@@ -18,6 +18,14 @@
 
 namespace gbs {
 
+// Block-rows (strips) of more tiles (entries) than kHubTiles (kHubStripNnz)
+// go to the hub passes of the SpMM / BMM (packer): the mean of a power-law
+// graph's tile-4 block-rows is ~40 tiles, its largest hubs have thousands.
+// Matrices of fewer than kHubMinBlockRows block-rows run in one pass.
+constexpr int kHubTiles = 256;
+constexpr int kHubStripNnz = 256;
+constexpr int kHubMinBlockRows = 1024;
+
 template <int TS> struct TileT;
 template <> struct TileT<4> { using T = uint8_t; };
 template <> struct TileT<8> { using T = uint8_t; };
@@ -35,7 +43,8 @@ template <int TS, bool FILL>
 __global__ void __launch_bounds__(256)
     k_b2sr_pack(int nrows, int ncols, int mb, const int *__restrict__ rowptr,
                 const int *__restrict__ colind, int *__restrict__ counts, const int *__restrict__ brp,
-                int *__restrict__ bcol, typename TileT<TS>::T *__restrict__ bval, int *__restrict__ err) {
+                int *__restrict__ bcol, typename TileT<TS>::T *__restrict__ bval, int *__restrict__ err,
+                int hub_min) {
   using VT = typename TileT<TS>::T;
   constexpr int G = 32 / TS;
   const int lane = threadIdx.x & 31;
@@ -43,6 +52,11 @@ __global__ void __launch_bounds__(256)
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long strip = gw * G + g;
   if (strip >= mb) return;  // the whole group leaves together
+  if (hub_min > 0) {  // strips of more entries belong to the hub pass
+    const long long r0 = strip * TS;
+    const long long r1 = r0 + TS < nrows ? r0 + TS : nrows;
+    if (__ldg(rowptr + r1) - __ldg(rowptr + r0) > hub_min) return;
+  }
   const unsigned gmask = (TS == 32) ? 0xffffffffu : (((1u << TS) - 1u) << (g * TS));
   const long long row = strip * TS + r;
   int p = 0, e = 0;
@@ -89,6 +103,150 @@ __global__ void __launch_bounds__(256)
   if (!FILL && r == 0) counts[strip] = cnt;
 }
 
+// Hub strips: strips with thousands of entries walk their tile columns one
+// at a time above, a chain of dependent loads per tile column.  Here one CTA
+// takes such a strip: every thread marks the tile columns of its entries in
+// a shared-memory bitmap (atomicOr), the count is the bitmap's population;
+// the fill pass turns the bitmap into tile positions (prefix popcounts per
+// word), writes the tile columns in ascending order and ORs every entry's
+// bit into its tile row with 32-bit global atomics (the strip's tile rows are
+// zeroed first).  Same output as the lane-group walk.  hubs = [count, strip
+// ids ...]; strips taken grid-stride.
+__global__ void k_find_hub_strips(const int *__restrict__ rowptr, int nrows, int mb, int ts, int min_nnz,
+                                  int *__restrict__ hubs) {
+  const long long strip = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (strip >= mb) return;
+  const long long r0 = strip * ts;
+  const long long r1 = r0 + ts < nrows ? r0 + ts : nrows;
+  if (rowptr[r1] - rowptr[r0] > min_nnz) hubs[1 + atomicAdd(hubs, 1)] = (int)strip;
+}
+
+// Block-wide exclusive sum of one int per thread (256 threads); returns the
+// total through *total.
+__device__ __forceinline__ int block_exclusive_sum(int x, int *scratch, int *total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) scratch[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    int v = lane < 8 ? scratch[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane < 8) scratch[8 + lane] = v;  // inclusive warp totals
+  }
+  __syncthreads();
+  const int before = (w > 0 ? scratch[8 + w - 1] : 0) + inc - x;
+  *total = scratch[15];
+  __syncthreads();
+  return before;
+}
+
+template <int TS, bool FILL>
+__global__ void __launch_bounds__(256)
+    k_b2sr_pack_hubs(int nrows, int ncols, const int *__restrict__ rowptr, const int *__restrict__ colind,
+                     int *__restrict__ counts, const int *__restrict__ brp, int *__restrict__ bcol,
+                     uint32_t *__restrict__ bval32, int *__restrict__ err, const int *__restrict__ hubs, int words) {
+  using VT = typename TileT<TS>::T;
+  extern __shared__ uint32_t sm[];
+  uint32_t *bm = sm;                                          // tile-column bitmap
+  int *pre = reinterpret_cast<int *>(sm + words);             // fill: tiles before each word
+  int *srp = pre + (FILL ? words : 0);                        // the strip's row pointers
+  int *scratch = srp + TS + 1;                                // 16 ints
+  const int tid = threadIdx.x;
+  const int nh = hubs[0];
+  for (int h = blockIdx.x; h < nh; h += gridDim.x) {
+    const int strip = hubs[1 + h];
+    const int r0 = strip * TS;
+    const int nr = nrows - r0 < TS ? nrows - r0 : TS;
+    if (tid <= nr) srp[tid] = rowptr[r0 + tid];
+    for (int w = tid; w < words; w += 256) bm[w] = 0u;
+    __syncthreads();
+    const int eb = srp[0], ee = srp[nr];
+    for (int e = eb + tid; e < ee; e += 256) {
+      const int c = colind[e];
+      if (FILL && (c < 0 || c >= ncols)) continue;  // a CSR the count pass would have rejected
+      if (!FILL) {
+        int lo = 0, hi = nr - 1;  // row of e: last r with srp[r] <= e
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (srp[mid] <= e) lo = mid;
+          else hi = mid - 1;
+        }
+        if (c < 0 || c >= ncols || (e > srp[lo] && colind[e - 1] > c)) {
+          atomicOr(err, 1);
+          continue;
+        }
+      }
+      const int key = c / TS;
+      atomicOr(bm + (key >> 5), 1u << (key & 31));
+    }
+    __syncthreads();
+    if (!FILL) {
+      int cnt = 0;
+      for (int w = tid; w < words; w += 256) cnt += __popc(bm[w]);
+      int total = 0;
+      block_exclusive_sum(cnt, scratch, &total);
+      if (tid == 0) counts[strip] = total;
+    } else {
+      const int per = (words + 255) / 256;
+      const int w0 = tid * per < words ? tid * per : words;
+      const int w1 = w0 + per < words ? w0 + per : words;
+      int local = 0;
+      for (int w = w0; w < w1; ++w) local += __popc(bm[w]);
+      int total = 0;
+      int run = block_exclusive_sum(local, scratch, &total);
+      for (int w = w0; w < w1; ++w) {
+        pre[w] = run;
+        run += __popc(bm[w]);
+      }
+      const int out = brp[strip], end = brp[strip + 1];
+      // zero the strip's tile rows, then OR the entries' bits in
+      const long long wb = (long long)out * TS * (long long)sizeof(VT) / 4;
+      const long long nwords = (long long)(brp[strip + 1] - out) * TS * (long long)sizeof(VT) / 4;
+      for (long long i = tid; i < nwords; i += 256) bval32[wb + i] = 0u;
+      __syncthreads();
+      for (int w = tid; w < words; w += 256) {
+        uint32_t m = bm[w];
+        int t = out + pre[w];
+        while (m && t < end) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1u;
+          bcol[t++] = w * 32 + b;
+        }
+      }
+      for (int e = eb + tid; e < ee; e += 256) {
+        int lo = 0, hi = nr - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (srp[mid] <= e) lo = mid;
+          else hi = mid - 1;
+        }
+        const int c = colind[e];
+        if (c < 0 || c >= ncols) continue;
+        const int key = c / TS, w = key >> 5, b = key & 31;
+        const int t = out + pre[w] + __popc(bm[w] & ((1u << b) - 1u));
+        if (t >= end) continue;  // tile counts from another matrix
+        const uint32_t bit = 1u << (TS - 1 - (c % TS));
+        const long long byte = ((long long)t * TS + lo) * (long long)sizeof(VT);
+        atomicOr(bval32 + byte / 4, bit << (8 * (int)(byte % 4)));
+      }
+    }
+    __syncthreads();  // the next strip reuses the shared arrays
+  }
+}
+
+// The packer's hub pass is used while its bitmap and prefix arrays fit in
+// kHubPackSmem bytes of shared memory.
+constexpr int kHubPackSmem = 96 * 1024;
+
 template <int TS>
 gbs_status launch_pack(bool fill, int nrows, int ncols, int mb, const int *rowptr, const int *colind,
                        int *counts, const int *brp, int *bcol, void *bval, int *err, cudaStream_t s) {
@@ -97,13 +255,37 @@ gbs_status launch_pack(bool fill, int nrows, int ncols, int mb, const int *rowpt
   const int blocks = (int)((warps * 32 + 255) / 256);
   using VT = typename TileT<TS>::T;
   if (blocks == 0) return GBS_OK;
+  // hub pass: needs the bitmap in shared memory and 4-byte aligned tile rows
+  const long long words = (((long long)ncols + TS - 1) / TS + 31) / 32;
+  const size_t smem = sizeof(uint32_t) * (size_t)words * (fill ? 2 : 1) + sizeof(int) * (TS + 1 + 16);
+  const bool hub = mb >= kHubMinBlockRows && smem <= (size_t)kHubPackSmem &&
+                   (!fill || (reinterpret_cast<uintptr_t>(bval) & 3u) == 0);
+  DevBuf hubs;
+  if (hub) {
+    GBS_TRY(hubs.alloc(sizeof(int) * ((size_t)mb + 1), s));
+    GBS_CUDA_TRY(cudaMemsetAsync(hubs.p, 0, sizeof(int), s));
+    k_find_hub_strips<<<(mb + 255) / 256, 256, 0, s>>>(rowptr, nrows, mb, TS, kHubStripNnz, hubs.as<int>());
+    GBS_TRY(check_launch("k_find_hub_strips"));
+  }
+  const int hub_min = hub ? kHubStripNnz : 0;
   if (fill)
     k_b2sr_pack<TS, true><<<blocks, 256, 0, s>>>(nrows, ncols, mb, rowptr, colind, counts, brp, bcol,
-                                                 reinterpret_cast<VT *>(bval), err);
+                                                 reinterpret_cast<VT *>(bval), err, hub_min);
   else
     k_b2sr_pack<TS, false><<<blocks, 256, 0, s>>>(nrows, ncols, mb, rowptr, colind, counts, brp, bcol,
-                                                  reinterpret_cast<VT *>(bval), err);
-  return check_launch("k_b2sr_pack");
+                                                  reinterpret_cast<VT *>(bval), err, hub_min);
+  GBS_TRY(check_launch("k_b2sr_pack"));
+  if (!hub) return GBS_OK;
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  const void *fn = fill ? (const void *)&k_b2sr_pack_hubs<TS, true> : (const void *)&k_b2sr_pack_hubs<TS, false>;
+  if (smem > 48 * 1024) GBS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int iwords = (int)words;
+  uint32_t *bval32 = reinterpret_cast<uint32_t *>(bval);
+  const int *hp = hubs.as<int>();
+  void *args[] = {&nrows, &ncols, &rowptr, &colind, &counts, &brp, &bcol, &bval32, &err, &hp, &iwords};
+  GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(di.sm_count * 2), dim3(256), args, smem, s));
+  return GBS_OK;
 }
 
 gbs_status pack_dispatch(int ts, bool fill, int nrows, int ncols, int mb, const int *rowptr,
@@ -400,11 +582,6 @@ bool pick_ts(int dt, int F, bool vec16, B2srVariant *v) {
 
 bool is_aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-// Block-rows of more tiles than this go to the hub pass (the mean of a
-// power-law graph's tile-4 block-rows is ~40; its largest hubs have
-// thousands); matrices of fewer block-rows run in one pass.
-constexpr int kHubTiles = 256;
-constexpr int kHubMinBlockRows = 1024;
 
 // Per-call events (created and destroyed around one fork/join).
 struct Events {

@@ -150,6 +150,47 @@ def test_pack_rejects_bad_csr(cuda):
         ops.csr2b2sr(bad_range, 8)
 
 
+def hub_matrix(n=8192, m=9000, hub_row=4101, hub_deg=3000, seed=5):
+    """n x m CSR, 3 entries per row, one row of hub_deg entries (its strip
+    goes to the packer's hub pass)."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for r in range(n):
+        k = hub_deg if r == hub_row else 3
+        rows.append(np.sort(rng.choice(m, size=k, replace=False)))
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(x) for x in rows])
+    return rp, np.concatenate(rows).astype(np.int32)
+
+
+@pytest.mark.parametrize("ts", TILES)
+def test_pack_hub_strip_bit_exact(cuda, ts):
+    """A strip with thousands of entries (shared-memory bitmap pass) packs
+    exactly like the oracle, beside thousands of ordinary strips."""
+    n, m = 8192, 9000
+    rp, ci = hub_matrix(n, m)
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    assert np.array_equal(Ab.rowptr.cpu().numpy(), brp)
+    assert np.array_equal(Ab.colind.cpu().numpy(), bci)
+    assert np.array_equal(host_val(Ab), bv)
+
+
+def test_pack_hub_strip_rejects_bad_csr(cuda):
+    """The hub pass validates its strips like the lane-group walk."""
+    n, m = 8192, 9000
+    rp, ci = hub_matrix(n, m)
+    hub0 = int(rp[4101])
+    bad = ci.copy()
+    bad[hub0 + 10], bad[hub0 + 11] = ci[hub0 + 11], ci[hub0 + 10]  # descending pair in the hub row
+    with pytest.raises(_lib.GbsError, match="ascending"):
+        ops.csr2b2sr(dev_csr(n, m, rp, bad, cuda), 4)
+    bad = ci.copy()
+    bad[int(rp[4102]) - 1] = m  # last entry of the hub row out of range
+    with pytest.raises(_lib.GbsError, match="range"):
+        ops.csr2b2sr(dev_csr(n, m, rp, bad, cuda), 8)
+
+
 @pytest.mark.parametrize("gi", range(len(GRAPHS)))
 @pytest.mark.parametrize("F", [32, 64, 128, 256])
 def test_fbf_tile4_bitwise_reference_order(cuda, gi, F):
