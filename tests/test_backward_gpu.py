@@ -228,6 +228,27 @@ def test_planned_backward(cuda, dtype, parts):
         assert torch.equal(dB, dB1) and torch.equal(dv, dv1)
 
 
+@pytest.mark.parametrize("dtype, F", [(torch.float32, 4), (torch.float32, 200), (torch.float32, 1024),
+                                      (torch.bfloat16, 8), (torch.bfloat16, 136), (torch.bfloat16, 2048)])
+def test_planned_backward_widths(cuda, dtype, F):
+    """Feature widths across the backward variants (3 parts)."""
+    g = G.gcn_normalize(G.uniform_rows(3000, 12))
+    n = g.nrows
+    Gd = G.normal(F, 41, (n, F)).to(dtype).to(cuda)
+    Hd = G.normal(F, 42, (n, F)).to(dtype).to(cuda)
+    T = ops.CSRTranspose(dev(g, cuda, False))
+    tv = T.values(g.vals.to(cuda))
+    dB, dv = ops.BackwardPlan(T, tv, F, dtype, 3).run(Gd, Hd)
+    rp, ci, v = g.rowptr.numpy(), g.colind.numpy(), g.vals.numpy()
+    Gr, Hr = Gd.float().cpu().numpy(), Hd.float().cpu().numpy()
+    wrp, wci, wpm = oracle.csr_transpose(n, n, rp, ci)
+    ref, mag = oracle.csr_spmm_f64(wrp, wci, v[wpm], Gr)
+    assert oracle.rel_err(dB.cpu().numpy(), ref, mag)[0] <= 1e-5
+    refv = oracle.sddmm_f64(rp, ci, Gr, Hr)
+    S = sddmm_scale(rp, ci, Gr, Hr)
+    assert np.max(np.abs(dv.cpu().numpy() - refv) / np.maximum(S, 1e-30)) <= 1e-5
+
+
 def test_planned_backward_auto_parts_and_reuse(cuda):
     """Automatic part count (1 when dC fits in half of L2) and a plan reused
     across calls with a shared workspace."""

@@ -70,7 +70,8 @@ def test_matches_cusparse(cuda):
     assert rel <= 2e-6, rel
 
 
-@pytest.mark.parametrize("F", [1, 3, 4, 8, 16, 24, 32, 40, 64, 100, 128, 256, 512, 1024])
+@pytest.mark.parametrize("F", [1, 3, 4, 8, 16, 24, 32, 40, 64, 100, 128, 136, 152, 200, 252, 256, 260, 512,
+                               1024])
 def test_feature_widths_f32(cuda, F):
     g = small_graph(300, 257, 0.05, F, empty_rows=(0, 17, 299))
     B = G.normal(F, 1, (257, F))
@@ -86,7 +87,7 @@ def test_binary_values_null(cuda):
 
 
 @pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
-@pytest.mark.parametrize("F", [8, 32, 64, 256, 1024, 2048])
+@pytest.mark.parametrize("F", [8, 32, 64, 136, 200, 256, 264, 1024, 2048])
 def test_half_features(cuda, dtype, F):
     g = small_graph(257, 300, 0.04, F + 1)
     B32 = G.normal(F, 2, (300, F))
@@ -228,6 +229,18 @@ def test_column_partitioned_plan(cuda, parts, dtype):
     check_f32(g, B.float(), C)
     C2 = plan.run(B.to(cuda))  # reusable
     assert torch.equal(C, C2)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_column_partitioned_plan_f256(cuda, dtype):
+    """F = 256 (the half-warp variants run when a part's B slice fits in half
+    of L2): the automatic split and an explicit one against FP64."""
+    g = G.flickr_like()
+    B = G.normal(7, 12, (g.ncols, 256)).to(dtype)
+    A = dev_csr(g, cuda)
+    for parts in (0, 3):
+        plan = ops.SpmmPlan(A, 256, dtype, parts=parts)
+        check_f32(g, B.float(), plan.run(B.to(cuda)))
 
 
 def test_plan_auto_parts(cuda):
