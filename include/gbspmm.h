@@ -339,12 +339,14 @@ GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t 
  * AND-popc (XOR from row popcounts), 3 = tcgen05 tensor cores on the bits
  * expanded to FP8 {0, 1}, one CTA per 128 x 256 tile, 4 = the same MMAs in
  * a persistent warp-specialised kernel (one CTA per SM, two TMEM
- * accumulators so a tile's epilogue overlaps the next tile's MMAs).  3 and 4
- * are exact and allocate (M+N)*K bytes of temporaries, stream-ordered.
+ * accumulators so a tile's epilogue overlaps the next tile's MMAs), 5 = its
+ * cluster-pair form (two CTAs share each B block through TMA multicast).
+ * 3, 4 and 5 are exact and allocate (M+N)*K bytes of temporaries,
+ * stream-ordered.
  * 8192^3 XOR on GB300: 0.87 / 3.59 / 7.51 ms for 3 / 1 / 2. */
 GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
                       int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
-/* Number of bounded mbarrier waits that ran out in algo-3/4 launches of this
+/* Number of bounded mbarrier waits that ran out in algo-3/4/5 launches of this
  * process (0 in normal operation; each timeout also skips that tile's
  * stores).  Synchronises with the device. */
 GBS_API gbs_status gbs_bmm_tc_timeouts(int *count);

@@ -268,6 +268,45 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int
   *n0 = (local / gm) * TC_BN;
 }
 
+// Epilogue of one 128 x 256 tile held in TMEM accumulator b: warp quarter
+// q4 reads its 32 lanes (= rows m0 + 32 q4 + lane) 32 columns at a time and
+// writes the counts (int32 or float C).
+__device__ __forceinline__ void epilogue_tile(const BmmTcArgs &a, uint32_t tmem, int b, int q4, int lane, int m0,
+                                              int n0) {
+  const int Kbits = 32 * a.Kw;
+  const int row = m0 + q4 * 32 + lane;
+  const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
+#pragma unroll 1
+  for (int cb = 0; cb < TC_BN / 32; ++cb) {
+    uint32_t v[32];
+    tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
+    const int c0 = n0 + cb * 32;
+    if (row < a.M) {
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const int c = c0 + q;
+        if (c >= a.N) break;
+        int x[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int andc = (int)__uint_as_float(v[q + e]);
+          int val = andc;
+          if (a.mode != 1) {
+            const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
+            val = a.mode == 0 ? xr : Kbits - 2 * xr;
+          }
+          x[e] = val;
+        }
+        if (a.Cf)
+          *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
+              make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
+        else
+          *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
+      }
+    }
+  }
+}
+
 // Persistent, warp-specialised version: one CTA per SM walks output tiles
 // tile = blockIdx.x, blockIdx.x + gridDim.x, ...  Warp 0 (one thread) feeds
 // the shared-memory ring with TMA, warp 1 (one thread) issues the MMAs, warps
@@ -370,7 +409,6 @@ __global__ void __launch_bounds__(192, 1)
   } else {
     // epilogue warps 2..5: TMEM lane quarter = warp % 4
     const int q4 = warp & 3;
-    const int Kbits = 32 * a.Kw;
     int i = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
       const int b = i & 1, u = i >> 1;
@@ -383,37 +421,7 @@ __global__ void __launch_bounds__(192, 1)
       if (!go) break;
       int m0, n0;
       tile_origin(t, tiles_m, tiles_n, &m0, &n0);
-      const int row = m0 + q4 * 32 + lane;
-      const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
-#pragma unroll 1
-      for (int cb = 0; cb < TC_BN / 32; ++cb) {
-        uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
-        const int c0 = n0 + cb * 32;
-        if (row < a.M) {
-#pragma unroll
-          for (int q = 0; q < 32; q += 4) {
-            const int c = c0 + q;
-            if (c >= a.N) break;
-            int x[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int andc = (int)__uint_as_float(v[q + e]);
-              int val = andc;
-              if (a.mode != 1) {
-                const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
-                val = a.mode == 0 ? xr : Kbits - 2 * xr;
-              }
-              x[e] = val;
-            }
-            if (a.Cf)
-              *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
-                  make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
-            else
-              *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
-          }
-        }
-      }
+      epilogue_tile(a, tmem, b, q4, lane, m0, n0);
       tc_fence_before();
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty + b)) : "memory");
@@ -421,6 +429,176 @@ __global__ void __launch_bounds__(192, 1)
   }
   tc_fence_before();
   __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * TC_BN) : "memory");
+  }
+}
+
+// Cluster-pair version of the persistent kernel: the two CTAs of a cluster
+// compute the two 128 x 256 tiles of a 256 x 256 pair tile that share their
+// B block.  Each CTA loads its own A slice and half of the B slice, the B
+// half multicast into both CTAs' shared memory (TMA .multicast::cluster), so
+// an SM pulls 32 KiB from L2 per K step instead of 48 KiB.  A ring slot may
+// be refilled only when both CTAs' MMAs have read it: every MMA batch
+// commits to the slot's empty barrier in both CTAs (count 2).  Full barriers
+// expect 48 KiB: the own A, the own B half and the peer's.  A cluster
+// barrier after the barrier set-up (before any multicast) and one before
+// exit (after each producer has seen its last copies land and its empty
+// barriers receive both CTAs' last commits) keep every remote write and
+// arrive inside the lifetime of the CTA it targets.  All waits are bounded.
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1)
+    k_bmm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh, BmmTcArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t *sA = base;
+  uint8_t *sB = base + TC_STAGES * TC_A_BYTES;
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + TC_STAGES * TC_B_BYTES);
+  uint64_t *empty = full + TC_STAGES;
+  uint64_t *tfull = empty + TC_STAGES;  // [2]
+  uint64_t *tempty = tfull + 2;         // [2]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rank = (int)cluster_ctarank();
+  const int cid = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
+  const int tiles_n = (a.N + TC_BN - 1) / TC_BN, tiles_m = (a.M + TC_BM - 1) / TC_BM;
+  const int pairs_m = (tiles_m + 1) / 2;
+  const int pairs = pairs_m * tiles_n;
+  const int nk = a.Kp / TC_BK;
+  constexpr uint16_t kBoth = 3;
+  constexpr int kHalfB = TC_B_BYTES / 2;
+
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 2);  // both CTAs' MMA commits
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull + b, 1);
+      mbar_init(tempty + b, 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2u * TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  __syncwarp();
+  cluster_sync_all();  // the peer's barriers exist before any multicast reaches them
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;
+      for (int t = cid; t < pairs && !s_fail; t += nclusters) {
+        int m0p, n0;
+        tile_origin(t, pairs_m, tiles_n, &m0p, &n0);
+        const int m0 = (2 * (m0p / TC_BM) + rank) * TC_BM;
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % TC_STAGES, r = g / TC_STAGES;
+          if (g >= TC_STAGES && !mbar_wait(empty + s, (uint32_t)((r - 1) & 1), a.err)) {
+            s_fail = 1;
+            break;
+          }
+          mbar_expect_tx(full + s, TC_A_BYTES + TC_B_BYTES);
+          tma_load_2d(sA + s * TC_A_BYTES, &tmA, kb * TC_BK, m0, full + s);
+          tma_load_2d_mc(sB + s * TC_B_BYTES + rank * kHalfB, &tmBh, kb * TC_BK, n0 + rank * (TC_BN / 2), full + s,
+                         kBoth);
+        }
+      }
+      // Before leaving: the last copies into this CTA have landed and both
+      // CTAs' MMAs have released the last slots (their commits reach this
+      // CTA's barriers).
+      for (int q = g - TC_STAGES < 0 ? 0 : g - TC_STAGES; q < g; ++q) {
+        const uint32_t ph = (uint32_t)((q / TC_STAGES) & 1);
+        if (!mbar_try_wait(full + q % TC_STAGES, ph)) mbar_wait(full + q % TC_STAGES, ph, a.err);
+        if (!mbar_try_wait(empty + q % TC_STAGES, ph)) mbar_wait(empty + q % TC_STAGES, ph, a.err);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int g = 0, i = 0;
+      for (int t = cid; t < pairs && !s_fail; t += nclusters, ++i) {
+        const int b = i & 1, u = i >> 1;
+        if (u >= 1 && !mbar_wait(tempty + b, (uint32_t)((u - 1) & 1), a.err)) {
+          s_fail = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % TC_STAGES, r = g / TC_STAGES;
+          if (!mbar_wait(full + s, (uint32_t)(r & 1), a.err)) {
+            s_fail = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t ad = sdesc_k_sw128(smem_u32(sA + s * TC_A_BYTES));
+          const uint64_t bd = sdesc_k_sw128(smem_u32(sB + s * TC_B_BYTES));
+#pragma unroll
+          for (int k = 0; k < TC_BK / 32; ++k) mma_f8(acc, ad + 2 * k, bd + 2 * k, TC_IDESC, (kb | k) != 0 ? 1u : 0u);
+          mma_commit_mc(empty + s, kBoth);
+        }
+        mma_commit(tfull + b);
+        if (s_fail) break;
+      }
+    }
+  } else {
+    const int q4 = warp & 3;
+    int i = 0;
+    for (int t = cid; t < pairs; t += nclusters, ++i) {
+      const int b = i & 1, u = i >> 1;
+      int go = 0;
+      if (lane == 0) go = mbar_wait(tfull + b, (uint32_t)(u & 1), a.err) && !s_fail;
+      go = __shfl_sync(0xffffffffu, go, 0);
+      tc_fence_after();
+      if (!go) break;
+      int m0p, n0;
+      tile_origin(t, pairs_m, tiles_n, &m0p, &n0);
+      const int m0 = (2 * (m0p / TC_BM) + rank) * TC_BM;
+      epilogue_tile(a, tmem, b, q4, lane, m0, n0);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty + b)) : "memory");
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  __syncwarp();
+  cluster_sync_all();  // no remote write or arrive can target this CTA any more
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
@@ -504,8 +682,11 @@ gbs_status make_map(CUtensorMap *map, void *base, int rows, int Kp, int box_rows
 
 static __device__ int g_bmm_tc_err;
 
+// launch forms of bmm_tc_run
+constexpr int kTcPerTile = 0, kTcPersistent = 1, kTcPair = 2;
+
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
-                      int ldc, cudaStream_t s, bool persistent) {
+                      int ldc, cudaStream_t s, int form) {
   GBS_REQUIRE(M % 4 == 0 && N % 4 == 0 && ldc % 4 == 0, "bmm tc: M, N (and ldc) must be multiples of 4");
   GBS_REQUIRE((long long)Kw * 32 < (1ll << 24), "bmm tc: K must be < 2^24 bits (exact FP32 accumulation)");
   const int Kp = (Kw * 32 + TC_BK - 1) / TC_BK * TC_BK;
@@ -522,13 +703,15 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   GBS_TRY(check_launch("bmm tc prologue"));
   CUtensorMap ma, mb;
   GBS_TRY(make_map(&ma, A8.p, M, Kp, TC_BM));
-  GBS_TRY(make_map(&mb, B8.p, N, Kp, TC_BN));
+  GBS_TRY(make_map(&mb, B8.p, N, Kp, form == kTcPair ? TC_BN / 2 : TC_BN));
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
     attr_err = cudaFuncSetAttribute(k_bmm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (attr_err == cudaSuccess)
       attr_err = cudaFuncSetAttribute(k_bmm_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_bmm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   });
   if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(k_bmm_tc)");
   int *err = nullptr;
@@ -537,7 +720,28 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   const int tiles = ((N + TC_BN - 1) / TC_BN) * ((M + TC_BM - 1) / TC_BM);
   DeviceInfo di;
   GBS_TRY(device_info(&di));
-  if (persistent) {
+  if (form == kTcPair) {
+    // clusters of 2 CTAs, as many as can be resident at once
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(192);
+    cfg.dynamicSmemBytes = TC_SMEM;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(2 * (unsigned)di.sm_count);
+    int max_clusters = 0;
+    GBS_CUDA_TRY(cudaOccupancyMaxActiveClusters(&max_clusters, (const void *)k_bmm_tc_pair, &cfg));
+    if (max_clusters < 1) return fail(GBS_ERR_UNSUPPORTED, "bmm tc: no CTA pair fits on this device");
+    const int pairs = ((N + TC_BN - 1) / TC_BN) * (((M + TC_BM - 1) / TC_BM + 1) / 2);
+    const int clusters = pairs < max_clusters ? pairs : max_clusters;
+    cfg.gridDim = dim3(2 * (unsigned)clusters);
+    GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_bmm_tc_pair, ma, mb, args));
+  } else if (form == kTcPersistent) {
     const int grid = tiles < di.sm_count ? tiles : di.sm_count;
     k_bmm_tc_persist<<<grid, 192, TC_SMEM, s>>>(ma, mb, args);
   } else {

@@ -1,8 +1,10 @@
 """GPU tests of the tcgen05 binary GEMM (bits expanded to FP8 {0, 1},
 tcgen05.mma kind::f8f6f4 into TMEM, TMA-staged operands) in both launch
-forms -- one CTA per tile (algo 3) and the persistent warp-specialised
-kernel with two TMEM accumulators (algo 4, the default): bit-exact against
-the oracle, partial tiles, more tiles than SMs, and no bounded wait ran out."""
+forms -- one CTA per tile (algo 3), the persistent warp-specialised
+kernel with two TMEM accumulators (algo 4, the default) and its cluster-pair
+form with the B blocks multicast to both CTAs (algo 5): bit-exact against
+the oracle, partial tiles (odd tile-row counts leave a pair half empty),
+more tiles than SMs, and no bounded wait ran out."""
 import numpy as np
 import pytest
 import torch
@@ -17,7 +19,7 @@ def words(rng, kw, rows):
     return rng.integers(0, 2 ** 32, (kw, rows), dtype=np.uint64).astype(np.uint32)
 
 
-TC_ALGOS = [ops.BMM_ALGO_TC, ops.BMM_ALGO_TC_PERSIST]
+TC_ALGOS = [ops.BMM_ALGO_TC, ops.BMM_ALGO_TC_PERSIST, ops.BMM_ALGO_TC_PAIR]
 
 
 @pytest.mark.parametrize("algo", TC_ALGOS)
@@ -61,7 +63,8 @@ def test_default_is_persistent_tc(cuda):
     d = ops.bmm_b1(dA, dB, ops.BMM_XOR)
     p = ops.bmm_b1(dA, dB, ops.BMM_XOR, ops.BMM_ALGO_TC_PERSIST)
     t = ops.bmm_b1(dA, dB, ops.BMM_XOR, ops.BMM_ALGO_TC)
-    assert torch.equal(d, p) and torch.equal(d, t)
+    q = ops.bmm_b1(dA, dB, ops.BMM_XOR, ops.BMM_ALGO_TC_PAIR)
+    assert torch.equal(d, p) and torch.equal(d, t) and torch.equal(d, q)
     assert ops.bmm_tc_timeouts() == 0
 
 
