@@ -120,12 +120,12 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
                            float *d_C, void *d_workspace, size_t workspace_bytes,
                            gbs_stream_t stream);
 
-/* Column-partitioned plan.  When B is larger than L2, splitting A by column
- * ranges into `parts` pieces (0 = choose: B bytes / (L2 / 2), a power of
- * two <= 8, or 1 when B fits in L2 or rows of B are reused fewer than 8
- * times) and accumulating one merge-path pass per piece keeps each pass's
- * row gathers in L2 (FP32, 232,965 x 256 B on GB300: 8.0 ms -> 6.6 ms as 4
- * parts).  The plan copies A's pattern and values into the parts (values
+/* Column-partitioned plan.  When B is larger than half of L2, splitting A by
+ * column ranges into `parts` pieces (0 = choose: the smallest power of two
+ * <= 8 whose B slice fits in half of L2, or 1 when B already does or rows of
+ * B are reused fewer than 8 times) and accumulating one merge-path pass per
+ * piece keeps each pass's row gathers in L2 (232,965 x 256 B on GB300: FP32
+ * 8.0 ms -> 6.4 ms as 4 parts, BF16 5.4 ms -> 4.8 ms as 2 parts).  The plan copies A's pattern and values into the parts (values
  * captured at creation; rebuild after changing them); with one part it only
  * records the caller's arrays, which must outlive it.  Synchronises the
  * stream.  Workspace as gbs_csr_spmm_workspace_size(nrows, nnz, F, btype). */
@@ -343,7 +343,7 @@ GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t 
  * cluster-pair form (two CTAs share each B block through TMA multicast).
  * 3, 4 and 5 are exact and allocate (M+N)*K bytes of temporaries,
  * stream-ordered.
- * 8192^3 XOR on GB300: 0.87 / 3.59 / 7.51 ms for 3 / 1 / 2. */
+ * 8192^3 XOR on GB300: 0.39 / 0.38 / 0.60 / 3.59 / 7.51 ms for 4 / 5 / 3 / 1 / 2. */
 GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
                       int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
 /* Number of bounded mbarrier waits that ran out in algo-3/4/5 launches of this
