@@ -125,7 +125,8 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
  * <= 8 whose B slice fits in half of L2, or 1 when B already does or rows of
  * B are reused fewer than 8 times) and accumulating one merge-path pass per
  * piece keeps each pass's row gathers in L2 (232,965 x 256 B on GB300: FP32
- * 8.0 ms -> 6.4 ms as 4 parts, BF16 5.4 ms -> 4.8 ms as 2 parts).  The plan copies A's pattern and values into the parts (values
+ * 8.0 ms -> 6.4 ms as 4 parts, BF16 5.4 ms -> 4.8 ms as 2 parts).  The
+ * plan copies A's pattern and values into the parts (values
  * captured at creation; rebuild after changing them); with one part it only
  * records the caller's arrays, which must outlive it.  Synchronises the
  * stream.  Workspace as gbs_csr_spmm_workspace_size(nrows, nnz, F, btype). */
