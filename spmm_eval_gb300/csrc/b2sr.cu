@@ -796,6 +796,75 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
   bmm_block_row<TS, WMAX, R, BmmShape<WMAX>::U, 2>(a, br, (int)(gw % NG), lane, lists[threadIdx.x >> 5]);
 }
 
+// One warp, one tile row `row` of a hub block-row.  The entries of 4 groups
+// that set the row's bit are compacted into `list`; the feature rows of 32
+// listed entries are then loaded in one round with the lanes spread over
+// (entry, word) -- 32 / WMAX entries per warp-wide load, so a round needs
+// WMAX loads per lane and no more registers -- and each word is broadcast to
+// the lanes by a shuffle when its bits are counted.  The chain of dependent
+// round trips is (entries / 32) deep instead of (entries / U).
+template <int TS, int WMAX>
+__device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list) {
+  constexpr int G = 4;
+  constexpr int TPG = 32 / TS;
+  constexpr int TPS = TPG * G;
+  constexpr int EPL = 32 / WMAX;  // entries per warp-wide load
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int cnt[WMAX];
+  int deg = 0;
+#pragma unroll
+  for (int k = 0; k < WMAX; ++k) cnt[k] = 0;
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int j = lane % TS, l = lane / TS;
+  const int shift = 31 - lane;
+  const int my_e = lane / WMAX, my_w = lane % WMAX;  // (entry, word) this lane loads
+  for (int s0 = tb; s0 < te; s0 += TPS) {
+    int n = 0;
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int t = s0 + g * TPG + l;
+      int col = 0;
+      bool set = false;
+      if (t < te) {
+        col = __ldg(a.colind + t) * TS + j;
+        set = (tile_row<TS>(a.val, (size_t)t, row) >> (TS - 1 - j)) & 1u;
+      }
+      const unsigned act = __ballot_sync(0xffffffffu, set);
+      if (set) list[n + __popc(act & lt_mask)] = make_int2(col, 0);
+      n += __popc(act);
+    }
+    __syncwarp();
+    for (int k0 = 0; k0 < n; k0 += 32) {
+      uint32_t w[WMAX];
+#pragma unroll
+      for (int it = 0; it < WMAX; ++it) {
+        const int u = k0 + it * EPL + my_e;
+        w[it] = (u < n && my_w < a.W) ? __ldg(a.X + (size_t)list[u].x * a.W + my_w) : 0u;
+      }
+      const int m = min(32, n - k0);
+      deg += m;
+#pragma unroll
+      for (int it = 0; it < WMAX; ++it)
+#pragma unroll
+        for (int e = 0; e < EPL; ++e) {
+          if (it * EPL + e >= m) break;  // warp-uniform
+#pragma unroll
+          for (int k = 0; k < WMAX; ++k)
+            cnt[k] += (int)((__shfl_sync(0xffffffffu, w[it], e * WMAX + k) >> shift) & 1u);
+        }
+    }
+    __syncwarp();
+  }
+  const long long orow = br * TS + row;
+  if (orow >= a.nrows) return;
+  int32_t *dst = a.C + (size_t)orow * a.F;
+#pragma unroll
+  for (int k = 0; k < WMAX; ++k) {
+    const int c = k * 32 + lane;
+    if (c < a.F) dst[c] = a.signed_form ? 2 * cnt[k] - deg : cnt[k];
+  }
+}
+
 // Hub pass: one warp per (hub block-row, tile row), items grid-stride.
 template <int TS, int WMAX>
 __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
@@ -806,7 +875,7 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
   __shared__ int2 lists[8][32 * 4];
   for (long long it = gw; it < items; it += nw) {
     const long long br = __ldg(a.hubs + 1 + it / TS);
-    bmm_block_row<TS, WMAX, 1, 2 * BmmShape<WMAX>::U, 4>(a, br, (int)(it % TS), lane, lists[threadIdx.x >> 5]);
+    bmm_hub_row<TS, WMAX>(a, br, (int)(it % TS), lane, lists[threadIdx.x >> 5]);
   }
 }
 

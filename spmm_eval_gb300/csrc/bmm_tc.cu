@@ -9,15 +9,19 @@
 // the FP32 accumulation is exact; XOR counts come from row popcounts as
 // popc(a) + popc(b) - 2 and(a, b).
 //
-// Kernel: one 128-thread CTA per 128 x 256 output tile.  Thread 0 of warp 0
-// streams 128-byte K slices of A (128 rows) and B (256 rows) into a 4-stage
-// shared-memory ring with TMA (cp.async.bulk.tensor, 128B swizzle,
-// mbarrier complete_tx); thread 0 of warp 1 issues four K=32 MMAs per slice
-// (tcgen05.mma, cta_group::1, M=128, N=256) and releases each slot with
-// tcgen05.commit; after the last slice all four warps read their 32 TMEM
-// lanes (= output rows) with tcgen05.ld and write int32 C.  Every mbarrier
-// wait is bounded: on timeout the kernel records an error flag, skips the
-// remaining work, frees its tensor memory and returns.
+// Three launch forms share the tile machinery.  k_bmm_tc: one 128-thread
+// CTA per 128 x 256 output tile.  Thread 0 of warp 0 streams 128-byte K
+// slices of A (128 rows) and B (256 rows) into a 4-stage shared-memory ring
+// with TMA (cp.async.bulk.tensor, 128B swizzle, mbarrier complete_tx);
+// thread 0 of warp 1 issues four K=32 MMAs per slice (tcgen05.mma,
+// cta_group::1, M=128, N=256) and releases each slot with tcgen05.commit;
+// after the last slice all four warps read their 32 TMEM lanes (= output
+// rows) with tcgen05.ld and write int32 C.  k_bmm_tc_persist (the default):
+// the same roles in a persistent warp-specialised CTA per SM with two TMEM
+// accumulators.  k_bmm_tc_pair: the persistent kernel on CTA pairs sharing
+// B blocks by TMA multicast.  Every mbarrier wait is bounded: on timeout the
+// kernel records an error flag, skips the remaining work, frees its tensor
+// memory and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -126,6 +130,45 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Epilogue of one 128 x 256 tile held in TMEM accumulator b: warp quarter
+// q4 reads its 32 lanes (= rows m0 + 32 q4 + lane) 32 columns at a time and
+// writes the counts (int32 or float C).
+__device__ __forceinline__ void epilogue_tile(const BmmTcArgs &a, uint32_t tmem, int b, int q4, int lane, int m0,
+                                              int n0) {
+  const int Kbits = 32 * a.Kw;
+  const int row = m0 + q4 * 32 + lane;
+  const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
+#pragma unroll 1
+  for (int cb = 0; cb < TC_BN / 32; ++cb) {
+    uint32_t v[32];
+    tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
+    const int c0 = n0 + cb * 32;
+    if (row < a.M) {
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        const int c = c0 + q;
+        if (c >= a.N) break;
+        int x[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int andc = (int)__uint_as_float(v[q + e]);
+          int val = andc;
+          if (a.mode != 1) {
+            const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
+            val = a.mode == 0 ? xr : Kbits - 2 * xr;
+          }
+          x[e] = val;
+        }
+        if (a.Cf)
+          *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
+              make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
+        else
+          *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128, 1)
     k_bmm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, BmmTcArgs a) {
   extern __shared__ uint8_t smem_raw[];
@@ -208,41 +251,7 @@ __global__ void __launch_bounds__(128, 1)
   if (lane == 0) have = mbar_wait(accf, 0, a.err) && !s_fail;
   have = __shfl_sync(0xffffffffu, have, 0);
   tc_fence_after();
-  if (have) {
-    const int row = m0 + warp * 32 + lane;
-    const int Kbits = 32 * a.Kw;
-    const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
-#pragma unroll 1
-    for (int cb = 0; cb < TC_BN / 32; ++cb) {
-      uint32_t v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
-      const int c0 = n0 + cb * 32;
-      if (row < a.M) {
-#pragma unroll
-        for (int q = 0; q < 32; q += 4) {
-          const int c = c0 + q;
-          if (c >= a.N) break;
-          int x[4];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int andc = (int)__uint_as_float(v[q + e]);
-            int val = andc;
-            if (a.mode != 1) {
-              const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
-              val = a.mode == 0 ? xr : Kbits - 2 * xr;
-            }
-            x[e] = val;
-          }
-          if (a.Cf) {
-            *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
-                make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
-          } else {
-            *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
-          }
-        }
-      }
-    }
-  }
+  if (have) epilogue_tile(a, tmem, 0, warp, lane, m0, n0);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -266,45 +275,6 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int
   const int local = t - grp * per_group;
   *m0 = (first + local % gm) * TC_BM;
   *n0 = (local / gm) * TC_BN;
-}
-
-// Epilogue of one 128 x 256 tile held in TMEM accumulator b: warp quarter
-// q4 reads its 32 lanes (= rows m0 + 32 q4 + lane) 32 columns at a time and
-// writes the counts (int32 or float C).
-__device__ __forceinline__ void epilogue_tile(const BmmTcArgs &a, uint32_t tmem, int b, int q4, int lane, int m0,
-                                              int n0) {
-  const int Kbits = 32 * a.Kw;
-  const int row = m0 + q4 * 32 + lane;
-  const int par = (a.mode != 1 && row < a.M) ? __ldg(a.pa + row) : 0;
-#pragma unroll 1
-  for (int cb = 0; cb < TC_BN / 32; ++cb) {
-    uint32_t v[32];
-    tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
-    const int c0 = n0 + cb * 32;
-    if (row < a.M) {
-#pragma unroll
-      for (int q = 0; q < 32; q += 4) {
-        const int c = c0 + q;
-        if (c >= a.N) break;
-        int x[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int andc = (int)__uint_as_float(v[q + e]);
-          int val = andc;
-          if (a.mode != 1) {
-            const int xr = par + __ldg(a.pb + c + e) - 2 * andc;
-            val = a.mode == 0 ? xr : Kbits - 2 * xr;
-          }
-          x[e] = val;
-        }
-        if (a.Cf)
-          *reinterpret_cast<float4 *>(a.Cf + (size_t)row * a.ldc + c) =
-              make_float4((float)x[0], (float)x[1], (float)x[2], (float)x[3]);
-        else
-          *reinterpret_cast<int4 *>(a.C + (size_t)row * a.ldc + c) = make_int4(x[0], x[1], x[2], x[3]);
-      }
-    }
-  }
 }
 
 // Persistent, warp-specialised version: one CTA per SM walks output tiles
