@@ -203,6 +203,19 @@ def test_host_buffer_pipelined(cuda, pinned, dtype, vals):
         check_f32(g, Bh.float(), C2, vals=vals)
 
 
+@pytest.mark.parametrize("dtype, F", [(torch.float32, 256), (torch.float32, 512), (torch.bfloat16, 512)])
+def test_host_buffer_wide_features(cuda, dtype, F):
+    """Host-buffer SpMM with B larger than half of L2 (FP32 F = 256, 512;
+    BF16 F = 512) against the FP64 oracle."""
+    g = G.flickr_like()
+    B32 = G.normal(F, 5, (g.ncols, F))
+    Bh = B32.to(dtype)
+    args = [t.pin_memory() for t in (g.rowptr, g.colind, g.vals, Bh)]
+    ctx = ops.HostSpmmContext()
+    C = ops.csr_spmm_host(*args, g.nrows, g.ncols, ctx=ctx)
+    check_f32(g, Bh.float(), C)
+
+
 def test_workspace_reused_across_shapes(cuda):
     """One workspace serving different shapes (different warp counts and
     slot widths) in sequence: each result still matches FP64."""
