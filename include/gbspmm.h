@@ -145,7 +145,7 @@ GBS_API gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *plan);
 /* Host-buffer form for callers that hold A, B and C in host memory, as the
  * reference's evalCSRSpmmFloatCuSPARSE does (test_spmm_full.cu:212-342):
  * copies in, C = A * B, copies out, and returns when h_C is filled.  A is
- * sent in row ranges of ~nnz/8 nonzeros so the copies overlap the kernels
+ * sent in row ranges of ~nnz/16 nonzeros so the copies overlap the kernels
  * (pinned host buffers are needed for the overlap; pageable ones work,
  * serialised).  ctx (optional) keeps device buffers, streams and events
  * between calls; with ctx == NULL each call allocates its buffers

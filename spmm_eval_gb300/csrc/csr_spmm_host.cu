@@ -22,7 +22,7 @@
 namespace gbs {
 namespace {
 
-constexpr int kChunks = 8;
+constexpr int kChunks = 16;
 
 struct StreamPair {
   cudaStream_t h2d = nullptr, d2h = nullptr;
