@@ -109,11 +109,41 @@ struct MergeKernel {
             else bv[u][c] = F_::zero();
           }
         }
+        if constexpr (SD) {
+          // each gathered chunk is widened once and feeds both the row sum
+          // and the dot product with the H row (even / odd columns as the
+          // two halves of FFMA2s, added at the end)
+          float sd[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
+          for (int u = 0; u < U; ++u) {
+            float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-          for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
-        if constexpr (SD) sddmm_round(a, base, u0, n_valid, sub, sl, h, bv);
+            for (int c = 0; c < CH; ++c) {
+              float x[VEC];
+              F_::widen(x, bv[u][c]);
+              if constexpr (VEC % 2 == 0) {
+#pragma unroll
+                for (int q = 0; q < VEC; q += 2) {
+                  fma2(bs[c][q], bs[c][q + 1], vv[u], x[q], x[q + 1]);
+                  fma2v(s0, s1, h[c][q], h[c][q + 1], x[q], x[q + 1]);
+                }
+              } else {
+#pragma unroll
+                for (int q = 0; q < VEC; ++q) {
+                  bs[c][q] = fmaf(vv[u], x[q], bs[c][q]);
+                  s0 = fmaf(h[c][q], x[q], s0);
+                }
+              }
+            }
+            sd[u] = s0 + s1;
+          }
+          sddmm_reduce(a, base, u0, n_valid, sub, sl, sd);
+        } else {
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
+        }
       }
 #pragma unroll
       for (int c = 0; c < CH; ++c)
@@ -129,31 +159,12 @@ struct MergeKernel {
         for (int q = 0; q < VEC; ++q) acc[c][q] += __shfl_xor_sync(0xffffffffu, acc[c][q], off);
   }
 
-  // Fused SDDMM for one round of U entries per sub-group: dot products of the
-  // gathered rows with the H row in registers, reduced over the LPR lanes by
-  // a multi-value butterfly ((U - 1) + log2(LPR / U) shuffles per U entries).
-  static __device__ __forceinline__ void sddmm_round(const MergeArgs &a, int base, int u0, int n_valid, int sub,
-                                                     int sl, const float (&h)[CH][VEC], const raw (&bv)[U][CH]) {
-    // per entry: even and odd columns summed as the two halves of FFMA2s,
-    // then added
-    float s[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-      for (int c = 0; c < CH; ++c) {
-        float x[VEC];
-        F_::widen(x, bv[u][c]);
-        if constexpr (VEC % 2 == 0) {
-#pragma unroll
-          for (int q = 0; q < VEC; q += 2) fma2v(s0, s1, h[c][q], h[c][q + 1], x[q], x[q + 1]);
-        } else {
-#pragma unroll
-          for (int q = 0; q < VEC; ++q) s0 = fmaf(h[c][q], x[q], s0);
-        }
-      }
-      s[u] = s0 + s1;
-    }
+  // Fused SDDMM for one round of U entries per sub-group: the per-lane
+  // partial dot products s[u] (gathered row . H row) are reduced over the LPR
+  // lanes by a multi-value butterfly ((U - 1) + log2(LPR / U) shuffles per U
+  // entries) and stored.
+  static __device__ __forceinline__ void sddmm_reduce(const MergeArgs &a, int base, int u0, int n_valid, int sub,
+                                                      int sl, float (&s)[U]) {
     int nv = U;
 #pragma unroll
     for (int off = LPR / 2; off >= 1; off >>= 1) {
