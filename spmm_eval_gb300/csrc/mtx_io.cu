@@ -17,6 +17,13 @@
 //     order (the reference's std::sort leaves their order unspecified).
 // Unlike the reference, a truncated file, an index outside the stated size,
 // a complex or dense ("array") file is an error instead of undefined state.
+//
+// Large files are parsed by several host threads: the entry section is cut
+// at line starts into one piece per thread, each piece is parsed on its own,
+// and the pieces are joined in file order (the first NZ entries count, the
+// first error among them is reported, as a front-to-back read would).  A
+// file whose entries span lines across a cut is parsed front to back.  The
+// per-row column sorts and the final gather run on the same threads.
 #include <algorithm>
 #include <cctype>
 #include <cerrno>
@@ -24,6 +31,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -88,6 +96,95 @@ struct Reader {
   }
 };
 
+// Entries parsed from one piece of the entry section [b, e): stops at the
+// end of the piece, after `limit` entries, or at the first bad entry.
+struct Piece {
+  std::vector<int> ri, ci;
+  std::vector<float> v;
+  int err = 0;         // 0 none, 1 row/col missing, 2 value missing, 3 outside the matrix
+  bool split = false;  // an entry continues past the end of the piece
+};
+
+// Next token start in [p, e) after whitespace, or e.
+inline const char *skip(const char *p, const char *e) {
+  while (p < e && std::isspace((unsigned char)*p)) ++p;
+  return p;
+}
+
+void parse_piece(const char *b, const char *e, bool last, int kind, long M, long N, long limit, Piece *out) {
+  const char *p = b;
+  out->ri.reserve((size_t)((e - b) / 8));
+  out->ci.reserve((size_t)((e - b) / 8));
+  out->v.reserve((size_t)((e - b) / 8));
+  long got = 0;
+  while (got < limit) {
+    char *end = nullptr;
+    p = skip(p, e);
+    if (p == e) {  // piece exhausted between entries
+      if (last) out->err = 1;
+      return;
+    }
+    const long r = std::strtol(p, &end, 10);
+    if (end == p) {
+      out->err = 1;
+      return;
+    }
+    p = skip(end, e);
+    if (p == e) {
+      if (last) out->err = 1;
+      else out->split = true;
+      return;
+    }
+    const long c = std::strtol(p, &end, 10);
+    if (end == p) {
+      out->err = 1;
+      return;
+    }
+    p = end;
+    float val = 1.0f;
+    if (kind != 2) {
+      p = skip(p, e);
+      if (p == e) {
+        if (last) out->err = 2;
+        else out->split = true;
+        return;
+      }
+      if (kind == 0) {
+        val = std::strtof(p, &end);
+      } else {
+        val = (float)(int)std::strtol(p, &end, 10);
+      }
+      if (end == p) {
+        out->err = 2;
+        return;
+      }
+      p = end;
+    }
+    if (r < 1 || r > M || c < 1 || c > N) {
+      out->err = 3;
+      return;
+    }
+    out->ri.push_back((int)(r - 1));
+    out->ci.push_back((int)(c - 1));
+    out->v.push_back(val);
+    ++got;
+  }
+}
+
+int host_threads() {
+  const unsigned hc = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(hc, 16u));
+}
+
+// Run f(t) for t in [0, T) on T threads (t = 0 on the calling thread).
+template <typename Fn>
+void run_threads(int T, Fn f) {
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) th.emplace_back(f, t);
+  f(0);
+  for (auto &x : th) x.join();
+}
+
 std::string lower(std::string s) {
   for (auto &c : s) c = (char)std::tolower((unsigned char)c);
   return s;
@@ -136,7 +233,46 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
 
   std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
   std::vector<float> v((size_t)NZ);
-  for (long e = 0; e < NZ; ++e) {
+  const int T = host_threads();
+  const char *body = rd.buf.data() + rd.pos, *bend = rd.buf.data() + rd.buf.size() - 1;
+  bool parallel_done = false;
+  if (T > 1 && bend - body > (8l << 20) && NZ > 0) {
+    // pieces start right after a newline
+    std::vector<const char *> cut(T + 1);
+    cut[0] = body;
+    cut[T] = bend;
+    for (int t = 1; t < T; ++t) {
+      const char *q = body + (bend - body) * t / T;
+      if (q < cut[t - 1]) q = cut[t - 1];
+      while (q < bend && *q != '\n') ++q;
+      cut[t] = q < bend ? q + 1 : bend;
+    }
+    std::vector<Piece> pc(T);
+    run_threads(T, [&](int t) { parse_piece(cut[t], cut[t + 1], t == T - 1, kind, M, N, NZ, &pc[t]); });
+    long have_n = 0;
+    bool split = false;
+    for (int t = 0; t < T && have_n < NZ; ++t) {
+      const long take = std::min((long)pc[t].ri.size(), NZ - have_n);
+      std::copy(pc[t].ri.begin(), pc[t].ri.begin() + take, ri.begin() + have_n);
+      std::copy(pc[t].ci.begin(), pc[t].ci.begin() + take, ci.begin() + have_n);
+      std::copy(pc[t].v.begin(), pc[t].v.begin() + take, v.begin() + have_n);
+      have_n += take;
+      if (have_n == NZ) break;
+      if (pc[t].split) {
+        split = true;
+        break;
+      }
+      if (pc[t].err == 3)
+        return fail(GBS_ERR_INVALID_ARG, "mtx: entry " + std::to_string(have_n + 1) + " outside the matrix");
+      if (pc[t].err == 2) return fail(GBS_ERR_INVALID_ARG, "mtx: missing value");
+      if (pc[t].err == 1) return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
+    }
+    if (!split) {
+      if (have_n < NZ) return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
+      parallel_done = true;
+    }
+  }
+  for (long e = 0; e < NZ && !parallel_done; ++e) {
     long r, cc;
     if (!rd.read_long(&r) || !rd.read_long(&cc))
       return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
@@ -161,9 +297,18 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
   for (long i = 0; i < M; ++i) rowptr[(size_t)i + 1] += rowptr[(size_t)i];
   std::vector<int> order((size_t)NZ), fill(rowptr.begin(), rowptr.end() - 1);
   for (long e = 0; e < NZ; ++e) order[(size_t)fill[(size_t)ri[(size_t)e]]++] = (int)e;
-  for (long i = 0; i < M; ++i)
-    std::stable_sort(order.begin() + rowptr[(size_t)i], order.begin() + rowptr[(size_t)i + 1],
-                     [&](int a, int b) { return ci[(size_t)a] < ci[(size_t)b]; });
+  // per-row sorts on T threads, rows split into ranges of ~NZ / T entries
+  std::vector<long> rcut(T + 1, M);
+  rcut[0] = 0;
+  for (int t = 1; t < T; ++t)
+    rcut[t] = std::lower_bound(rowptr.begin(), rowptr.end() - 1, (int)((long long)NZ * t / T)) - rowptr.begin();
+  for (int t = 1; t <= T; ++t) rcut[t] = std::max(rcut[t], rcut[t - 1]);
+  run_threads(NZ > (1l << 20) ? T : 1, [&](int t) {
+    const long i0 = NZ > (1l << 20) ? rcut[t] : 0, i1 = NZ > (1l << 20) ? rcut[t + 1] : M;
+    for (long i = i0; i < i1; ++i)
+      std::stable_sort(order.begin() + rowptr[(size_t)i], order.begin() + rowptr[(size_t)i + 1],
+                       [&](int a, int b) { return ci[(size_t)a] < ci[(size_t)b]; });
+  });
 
   out->nrows = (int)M;
   out->ncols = (int)N;
@@ -176,11 +321,14 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
     return fail(GBS_ERR_OOM, "mtx: host allocation failed");
   }
   std::memcpy(out->rowptr, rowptr.data(), sizeof(int) * ((size_t)M + 1));
-  for (long e = 0; e < NZ; ++e) {
-    const int k = order[(size_t)e];
-    out->colind[e] = ci[(size_t)k];
-    out->vals[e] = v[(size_t)k];
-  }
+  const int TG = NZ > (1l << 20) ? T : 1;
+  run_threads(TG, [&](int t) {
+    for (long e = NZ * t / TG; e < NZ * (t + 1) / TG; ++e) {
+      const int k = order[(size_t)e];
+      out->colind[e] = ci[(size_t)k];
+      out->vals[e] = v[(size_t)k];
+    }
+  });
   return GBS_OK;
 }
 

@@ -49,3 +49,54 @@ def test_reader_roundtrip_generated_graph(built_lib, tmp_path):
     nrows, ncols, rowptr, colind, vals = ops.read_mtx(f)
     assert np.array_equal(rowptr, g.rowptr.numpy()) and np.array_equal(colind, g.colind.numpy())
     assert np.all(vals == 1.0)
+
+
+def _big_file(tmp_path, name, n=60000, deg=20, seed=3, sep=" ", value=True, extra=""):
+    """A file of n * deg entries (> 8 MB, parsed by several threads) in
+    scrambled order, and the CSR a front-to-back read must give."""
+    rng = np.random.default_rng(seed)
+    rows = np.repeat(np.arange(n), deg)
+    cols = rng.integers(0, n, rows.size)
+    vals = rng.integers(-9, 10, rows.size).astype(np.float32) / 4
+    order = rng.permutation(rows.size)
+    r, c, v = rows[order], cols[order], vals[order]
+    kind = "real" if value else "pattern"
+    body = [f"%%MatrixMarket matrix coordinate {kind} general", f"{n} {n} {rows.size}"]
+    if value:
+        body += [f"{a + 1}{sep}{b + 1}{sep}{x:g}" for a, b, x in zip(r, c, v)]
+    else:
+        body += [f"{a + 1}{sep}{b + 1}" for a, b in zip(r, c)]
+    f = tmp_path / name
+    f.write_text("\n".join(body) + "\n" + extra)
+    key = np.lexsort((np.arange(r.size), c, r))  # by (row, col), file order on ties
+    rowptr = np.zeros(n + 1, np.int64)
+    rowptr[1:] = np.cumsum(np.bincount(r, minlength=n))
+    return f, rowptr, c[key], (v[key] if value else np.ones(r.size, np.float32))
+
+
+@pytest.mark.parametrize("sep, value", [(" ", True), (" ", False), ("\n", True)])
+def test_reader_large_file_threads(built_lib, tmp_path, sep, value):
+    """Several parse threads (and, with one token per line, the front-to-back
+    fallback when an entry spans a cut) give the front-to-back result; extra
+    entries and trailing junk after the stated count are ignored."""
+    f, rowptr, colind, vals = _big_file(tmp_path, "big.mtx", sep=sep, value=value, extra="1 1 1\njunk\n")
+    assert f.stat().st_size > 8 << 20
+    nrows, ncols, rp, ci, vv = ops.read_mtx(f)
+    assert np.array_equal(rp, rowptr) and np.array_equal(ci, colind)
+    assert np.array_equal(vv, vals)
+
+
+def test_reader_large_file_errors(built_lib, tmp_path):
+    """The first bad entry is reported by its position in the file, also when
+    it sits in a later thread's piece."""
+    f, *_ = _big_file(tmp_path, "big.mtx")
+    lines = f.read_text().split("\n")
+    bad = 2 + 1_000_000  # header lines + index of the bad entry
+    lines[bad] = "999999 1 1"
+    f.write_text("\n".join(lines))
+    with pytest.raises(_lib.GbsError, match="entry 1000001 outside"):
+        ops.read_mtx(f)
+    lines[bad] = "12 1 1"
+    f.write_text("\n".join(lines[:-50000]) + "\n")  # truncated
+    with pytest.raises(_lib.GbsError, match="fewer entries"):
+        ops.read_mtx(f)
