@@ -300,7 +300,6 @@ gbs_status pack_dispatch(int ts, bool fill, int nrows, int ncols, int mb, const 
   }
 }
 
-static size_t tile_elem_bytes(int ts) { return ts <= 8 ? 1 : (ts == 16 ? 2 : 4); }
 
 // counts -> bsrRowPtr (exclusive scan, total in [mb]) and nnzb / validity to
 // the host.

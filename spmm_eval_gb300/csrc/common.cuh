@@ -103,11 +103,6 @@ __device__ __forceinline__ float ld_stream_f32(const float *p) {
                : "l"(p));
   return v;
 }
-// Bulk prefetch of [p, p + bytes) into L2 (TMA unit; p 16-byte aligned,
-// bytes a multiple of 16).  Holds no registers while in flight.
-__device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
 // Output rows are written once and not re-read by the kernel.
 __device__ __forceinline__ void st_stream_f4(void *p, float4 v) {
   asm volatile("st.global.cs.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(v.x),

@@ -12,6 +12,7 @@
 #include "feat.cuh"
 #include "merge.cuh"
 #include "merge_kernel.cuh"
+#include "util.cuh"
 
 namespace gbs {
 
@@ -322,13 +323,8 @@ extern "C" gbs_status gbs_csr_spmm_f32(int nrows, int ncols, int nnz, const int 
   SpmmPlan p;
   GBS_TRY(spmm_plan(DT_F32, nrows, ncols, nnz, F, B, C, 0, &p));
   cudaStream_t s = (cudaStream_t)stream;
-  void *ws = nullptr;
-  GBS_CUDA_TRY(cudaMallocAsync(&ws, p.ws_bytes, s));
-  cudaError_t e = cudaMemsetAsync(ws, 0, p.ws_bytes, s);
-  gbs_status st = GBS_OK;
-  if (e != cudaSuccess) st = cuda_fail(e, "cudaMemsetAsync");
-  if (st == GBS_OK) st = spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws, s);
-  cudaError_t e2 = cudaFreeAsync(ws, s);
-  if (st == GBS_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaFreeAsync");
-  return st;
+  DevBuf ws;  // library pool, stream-ordered
+  GBS_TRY(ws.alloc(p.ws_bytes, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(ws.p, 0, p.ws_bytes, s));
+  return spmm_run(p, nrows, nnz, rowptr, colind, vals, B, F, C, ws.p, s);
 }

@@ -1,7 +1,7 @@
 // Device-wide scans and the stable key sort used by the packers and the
 // transpose, on CUB (header library shipped with the CUDA toolkit).  Kept in
-// one translation unit so CUB is compiled once.  Temporary storage is
-// stream-ordered (cudaMallocAsync / cudaFreeAsync).
+// one translation unit so CUB is compiled once.  Temporary storage comes from
+// the library's stream-ordered pool (DevBuf).
 #include <cub/cub.cuh>
 
 #include "common.cuh"
@@ -13,25 +13,9 @@ gbs_status exclusive_scan_i32(const int *in, int *out, int n, cudaStream_t s) {
   if (n <= 0) return GBS_OK;
   size_t tmp = 0;
   GBS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, n, s));
-  void *buf = nullptr;
-  GBS_CUDA_TRY(cudaMallocAsync(&buf, tmp, s));
-  cudaError_t e = cub::DeviceScan::ExclusiveSum(buf, tmp, in, out, n, s);
-  cudaError_t e2 = cudaFreeAsync(buf, s);
-  if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceScan::ExclusiveSum");
-  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
-  return GBS_OK;
-}
-
-gbs_status exclusive_scan_i64(const long long *in, long long *out, int n, cudaStream_t s) {
-  if (n <= 0) return GBS_OK;
-  size_t tmp = 0;
-  GBS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, n, s));
-  void *buf = nullptr;
-  GBS_CUDA_TRY(cudaMallocAsync(&buf, tmp, s));
-  cudaError_t e = cub::DeviceScan::ExclusiveSum(buf, tmp, in, out, n, s);
-  cudaError_t e2 = cudaFreeAsync(buf, s);
-  if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceScan::ExclusiveSum");
-  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+  DevBuf buf;
+  GBS_TRY(buf.alloc(tmp, s));
+  GBS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(buf.p, tmp, in, out, n, s));
   return GBS_OK;
 }
 
@@ -41,13 +25,10 @@ gbs_status stable_sort_pairs_i32(const int *keys_in, int *keys_out, const int *v
   size_t tmp = 0;
   GBS_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys_in, keys_out, vals_in, vals_out,
                                                n, 0, key_bits, s));
-  void *buf = nullptr;
-  GBS_CUDA_TRY(cudaMallocAsync(&buf, tmp, s));
-  cudaError_t e = cub::DeviceRadixSort::SortPairs(buf, tmp, keys_in, keys_out, vals_in, vals_out,
-                                                  n, 0, key_bits, s);
-  cudaError_t e2 = cudaFreeAsync(buf, s);
-  if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceRadixSort::SortPairs");
-  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+  DevBuf buf;
+  GBS_TRY(buf.alloc(tmp, s));
+  GBS_CUDA_TRY(cub::DeviceRadixSort::SortPairs(buf.p, tmp, keys_in, keys_out, vals_in, vals_out,
+                                               n, 0, key_bits, s));
   return GBS_OK;
 }
 

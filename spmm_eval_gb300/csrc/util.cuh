@@ -7,7 +7,6 @@ namespace gbs {
 
 // out[i] = sum in[0..i-1]; n elements.
 gbs_status exclusive_scan_i32(const int *in, int *out, int n, cudaStream_t s);
-gbs_status exclusive_scan_i64(const long long *in, long long *out, int n, cudaStream_t s);
 // Stable radix sort of (key, value) pairs on the low key_bits bits of key.
 gbs_status stable_sort_pairs_i32(const int *keys_in, int *keys_out, const int *vals_in,
                                  int *vals_out, int n, int key_bits, cudaStream_t s);
