@@ -75,6 +75,15 @@ typedef struct gbs_host_csr {
 
 GBS_API gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out);
 GBS_API void gbs_host_csr_free(gbs_host_csr *csr);
+/* Binary CSR cache, so a large .mtx is parsed once (the reference derives
+ * .bin cache names for the same purpose, readMtx.hpp:227-244, but never
+ * writes one).  Host byte order: "GBSCSR1\0", int32 nrows, ncols, nnz,
+ * has_vals, rowptr, colind, [vals].  write: vals NULL stores a pattern
+ * (read back as 1.0).  read: fills *out (free with gbs_host_csr_free); a
+ * truncated file, a row pointer that is not monotone or a column outside
+ * [0, ncols) is an error.  No counterpart in the reference's code path. */
+GBS_API gbs_status gbs_csr_write_bin(const char *path, const gbs_host_csr *csr);
+GBS_API gbs_status gbs_csr_read_bin(const char *path, gbs_host_csr *out);
 
 /* ------------------------------------------------------------------------
  * CSR SpMM  C = A * B   (A: nrows x ncols CSR, B: ncols x F, C: nrows x F)

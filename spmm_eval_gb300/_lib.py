@@ -44,6 +44,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_pool_trim": (st, []),
     "gbs_mtx_read": (st, [C.c_char_p, C.POINTER(HostCSR)]),
     "gbs_host_csr_free": (None, [C.POINTER(HostCSR)]),
+    "gbs_csr_write_bin": (st, [C.c_char_p, C.POINTER(HostCSR)]),
+    "gbs_csr_read_bin": (st, [C.c_char_p, C.POINTER(HostCSR)]),
     "gbs_csr_spmm_workspace_size": (st, [i32, i32, i32, i32, psz]),
     "gbs_csr_spmm_workspace_init": (st, [p, sz, p]),
     "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),

@@ -341,3 +341,77 @@ extern "C" void gbs_host_csr_free(gbs_host_csr *c) {
   c->colind = nullptr;
   c->vals = nullptr;
 }
+
+// ---------------------------------------------------------------------------
+// Binary CSR cache: parsing a large .mtx once and reloading its CSR.  Layout
+// (host byte order): 8-byte magic "GBSCSR1\0", int32 nrows, ncols, nnz,
+// has_vals, then rowptr[nrows + 1], colind[nnz] (int32) and, if has_vals,
+// vals[nnz] (float32).
+// ---------------------------------------------------------------------------
+namespace {
+const char kBinMagic[8] = {'G', 'B', 'S', 'C', 'S', 'R', '1', '\0'};
+}
+
+extern "C" gbs_status gbs_csr_write_bin(const char *path, const gbs_host_csr *csr) {
+  clear_error();
+  GBS_REQUIRE(path && csr, "csr bin: null argument");
+  GBS_REQUIRE(csr->nrows >= 0 && csr->ncols >= 0 && csr->nnz >= 0 && csr->rowptr, "csr bin: bad CSR");
+  GBS_REQUIRE(csr->nnz == 0 || csr->colind, "csr bin: null colind");
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(GBS_ERR_INVALID_ARG, std::string("csr bin: cannot create ") + path);
+  const int hdr[4] = {csr->nrows, csr->ncols, csr->nnz, csr->vals ? 1 : 0};
+  bool ok = std::fwrite(kBinMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int), 4, f) == 4 &&
+            std::fwrite(csr->rowptr, sizeof(int), (size_t)csr->nrows + 1, f) == (size_t)csr->nrows + 1 &&
+            std::fwrite(csr->colind, sizeof(int), (size_t)csr->nnz, f) == (size_t)csr->nnz;
+  if (ok && csr->vals) ok = std::fwrite(csr->vals, sizeof(float), (size_t)csr->nnz, f) == (size_t)csr->nnz;
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return fail(GBS_ERR_INVALID_ARG, std::string("csr bin: write failed: ") + path);
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_csr_read_bin(const char *path, gbs_host_csr *out) {
+  clear_error();
+  GBS_REQUIRE(path && out, "csr bin: null argument");
+  std::memset(out, 0, sizeof(*out));
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(GBS_ERR_INVALID_ARG, std::string("csr bin: cannot open ") + path);
+  char magic[8];
+  int hdr[4];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kBinMagic, 8) != 0 ||
+      std::fread(hdr, sizeof(int), 4, f) != 4) {
+    std::fclose(f);
+    return fail(GBS_ERR_INVALID_ARG, "csr bin: not a CSR cache file");
+  }
+  const int n = hdr[0], m = hdr[1], nnz = hdr[2], has_vals = hdr[3];
+  if (n < 0 || m < 0 || nnz < 0 || (has_vals != 0 && has_vals != 1)) {
+    std::fclose(f);
+    return fail(GBS_ERR_INVALID_ARG, "csr bin: corrupt header");
+  }
+  out->nrows = n;
+  out->ncols = m;
+  out->nnz = nnz;
+  out->rowptr = (int *)std::malloc(sizeof(int) * ((size_t)n + 1));
+  out->colind = (int *)std::malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+  out->vals = (float *)std::malloc(sizeof(float) * (size_t)(nnz > 0 ? nnz : 1));
+  if (!out->rowptr || !out->colind || !out->vals) {
+    std::fclose(f);
+    gbs_host_csr_free(out);
+    return fail(GBS_ERR_OOM, "csr bin: host allocation failed");
+  }
+  bool ok = std::fread(out->rowptr, sizeof(int), (size_t)n + 1, f) == (size_t)n + 1 &&
+            std::fread(out->colind, sizeof(int), (size_t)nnz, f) == (size_t)nnz;
+  if (ok && has_vals) ok = std::fread(out->vals, sizeof(float), (size_t)nnz, f) == (size_t)nnz;
+  if (ok && !has_vals)
+    for (int e = 0; e < nnz; ++e) out->vals[e] = 1.0f;
+  std::fclose(f);
+  // a CSR the rest of the library can trust
+  if (ok) ok = out->rowptr[0] == 0 && out->rowptr[n] == nnz;
+  for (int i = 0; ok && i < n; ++i) ok = out->rowptr[i] <= out->rowptr[i + 1];
+  for (int e = 0; ok && e < nnz; ++e) ok = out->colind[e] >= 0 && out->colind[e] < m;
+  if (!ok) {
+    gbs_host_csr_free(out);
+    std::memset(out, 0, sizeof(*out));
+    return fail(GBS_ERR_INVALID_ARG, "csr bin: truncated or inconsistent file");
+  }
+  return GBS_OK;
+}

@@ -490,12 +490,10 @@ def pool_trim() -> None:
     _lib.call("gbs_pool_trim")
 
 
-def read_mtx(path: str):
-    """(nrows, ncols, rowptr, colind, vals) as numpy arrays, with the
-    reference's readMtx + coo2csr semantics."""
+def _host_csr_arrays(fn: str, path) -> tuple:
     import numpy as np
     h = _lib.HostCSR()
-    _lib.call("gbs_mtx_read", str(path).encode(), C.byref(h))
+    _lib.call(fn, str(path).encode(), C.byref(h))
     try:
         n, nnz = h.nrows, h.nnz
         rowptr = np.ctypeslib.as_array(h.rowptr, shape=(n + 1,)).copy()
@@ -504,3 +502,29 @@ def read_mtx(path: str):
         return h.nrows, h.ncols, rowptr, colind, vals
     finally:
         _lib.load().gbs_host_csr_free(C.byref(h))
+
+
+def read_mtx(path) -> tuple:
+    """(nrows, ncols, rowptr, colind, vals) as numpy arrays, with the
+    reference's readMtx + coo2csr semantics."""
+    return _host_csr_arrays("gbs_mtx_read", path)
+
+
+def read_csr_bin(path) -> tuple:
+    """(nrows, ncols, rowptr, colind, vals) from a binary CSR cache file."""
+    return _host_csr_arrays("gbs_csr_read_bin", path)
+
+
+def write_csr_bin(path, nrows: int, ncols: int, rowptr, colind, vals=None) -> None:
+    """Write a host CSR (numpy arrays; vals None = pattern) as a binary
+    cache file (gbs_csr_write_bin)."""
+    import numpy as np
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colind, dtype=np.int32)
+    va = None if vals is None else np.ascontiguousarray(vals, dtype=np.float32)
+    h = _lib.HostCSR()
+    h.nrows, h.ncols, h.nnz = int(nrows), int(ncols), int(ci.size)
+    h.rowptr = rp.ctypes.data_as(C.POINTER(C.c_int))
+    h.colind = ci.ctypes.data_as(C.POINTER(C.c_int))
+    h.vals = va.ctypes.data_as(C.POINTER(C.c_float)) if va is not None else C.POINTER(C.c_float)()
+    _lib.call("gbs_csr_write_bin", str(path).encode(), C.byref(h))

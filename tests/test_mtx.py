@@ -100,3 +100,49 @@ def test_reader_large_file_errors(built_lib, tmp_path):
     f.write_text("\n".join(lines[:-50000]) + "\n")  # truncated
     with pytest.raises(_lib.GbsError, match="fewer entries"):
         ops.read_mtx(f)
+
+
+@pytest.mark.parametrize("with_vals", [True, False])
+def test_csr_bin_roundtrip(built_lib, tmp_path, with_vals):
+    """A CSR written to the binary cache reads back identically; a pattern
+    (no values) reads back as 1.0 like a pattern .mtx."""
+    f, rowptr, colind, vals = _big_file(tmp_path, "g.mtx", n=3000, deg=7, value=with_vals)
+    n, m, rp, ci, vv = ops.read_mtx(f)
+    b = tmp_path / "g.bin"
+    ops.write_csr_bin(b, n, m, rp, ci, vv if with_vals else None)
+    assert b.stat().st_size == 24 + 4 * (n + 1) + 4 * ci.size * (2 if with_vals else 1)
+    n2, m2, rp2, ci2, vv2 = ops.read_csr_bin(b)
+    assert (n2, m2) == (n, m)
+    assert np.array_equal(rp2, rp) and np.array_equal(ci2, ci)
+    assert np.array_equal(vv2, vv if with_vals else np.ones_like(vv))
+
+
+def test_csr_bin_empty(built_lib, tmp_path):
+    b = tmp_path / "e.bin"
+    ops.write_csr_bin(b, 5, 3, np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
+    n, m, rp, ci, vv = ops.read_csr_bin(b)
+    assert (n, m) == (5, 3) and np.array_equal(rp, np.zeros(6)) and ci.size == 0 and vv.size == 0
+
+
+def test_csr_bin_rejects_bad_files(built_lib, tmp_path):
+    """Wrong magic, truncation, a row pointer out of order and a column
+    outside [0, ncols) are errors, never a CSR handed to the kernels."""
+    b = tmp_path / "g.bin"
+    rp = np.array([0, 2, 3, 5], np.int32)
+    ci = np.array([0, 3, 1, 2, 3], np.int32)
+    ops.write_csr_bin(b, 3, 4, rp, ci, np.arange(5, dtype=np.float32))
+    good = b.read_bytes()
+    cases = {
+        "magic": b"XBSCSR1\0" + good[8:],
+        "trunc": good[:-3],
+        "header": good[:8] + np.array([3, 4, 5, 7], np.int32).tobytes() + good[24:],
+        "rowptr": good[:24] + np.array([0, 3, 2, 5], np.int32).tobytes() + good[40:],
+        "column": good[:40] + np.array([0, 4, 1, 2, 3], np.int32).tobytes() + good[60:],
+    }
+    for name, data in cases.items():
+        bad = tmp_path / f"{name}.bin"
+        bad.write_bytes(data)
+        with pytest.raises(_lib.GbsError, match="csr bin"):
+            ops.read_csr_bin(bad)
+    with pytest.raises(_lib.GbsError, match="cannot open"):
+        ops.read_csr_bin(tmp_path / "missing.bin")
