@@ -55,8 +55,44 @@ template <int DT, int VEC, int LPR, int CH, int U, bool SD = false>
 struct MergeKernel {
   static constexpr int NSUB = 32 / LPR;
   static constexpr int KPS = LPR;  // nonzeros per sub-group in a batch of 32
+  // Blocked summation (a fresh partial per batch of 32 nonzeros) for FP32
+  // features only: it holds the FP32 error bound on rows of 20,000 entries,
+  // while for 16-bit features the input rounding dominates and the second
+  // set of accumulators would cost a CTA per SM (32 -> 24 warps).
+  static constexpr bool BLK = DT == DT_F32;
   using F_ = Feat<DT, VEC>;
   using raw = typename F_::raw;
+
+  // One forward round: U nonzeros per sub-group, entries u0 .. u0 + U - 1
+  // of the sub-group's share of the batch.  TAIL: some entries may lie past
+  // n_valid (their loads are skipped and their values zeroed); otherwise
+  // every entry exists and the loads go out unpredicated.  Lanes whose chunk
+  // lies past the row gather the row's last chunk; their sums are never
+  // stored.
+  template <bool TAIL>
+  static __device__ __forceinline__ void round(const MergeArgs &a, int u0, int n_valid, int sub, int sl,
+                                               int my_col, float my_val, float (&bs)[CH][VEC]) {
+    raw bv[U][CH];
+    float vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = ((u0 + u) * NSUB + sub) & 31;
+      const int col = __shfl_sync(0xffffffffu, my_col, k);
+      const float v = __shfl_sync(0xffffffffu, my_val, k);
+      const bool ok = !TAIL || (u0 + u) * NSUB + sub < n_valid;
+      vv[u] = ok ? v : 0.f;
+      const size_t rowbase = (size_t)col * (size_t)a.ldb;
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        if (ok) bv[u][c] = F_::load(a.B, rowbase + (size_t)(min(c * LPR + sl, a.nvec - 1) * VEC));
+        else bv[u][c] = F_::zero();
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
+  }
 
   // Sum nonzeros [jb, je) of one row into acc (this lane's columns, this
   // lane's sub-group share).
@@ -70,46 +106,60 @@ struct MergeKernel {
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
 
+    int nx_col = 0;
+    float nx_val = 0.f;
+    if (jb + lane < je) {
+      nx_col = ld_stream_i32(a.colind + jb + lane);
+      nx_val = a.vals ? ld_stream_f32(a.vals + jb + lane) : 1.f;
+    }
     for (int base = jb; base < je; base += 32) {
       const int n_valid = min(32, je - base);
-      int my_col = 0;
-      float my_val = 0.f;
-      if (lane < n_valid) {
-        my_col = ld_stream_i32(a.colind + base + lane);
-        my_val = a.vals ? ld_stream_f32(a.vals + base + lane) : 1.f;
+      const int my_col = nx_col;
+      const float my_val = nx_val;
+      // the next batch of this row is loaded while this one is gathered
+      if (base + 32 + lane < je) {
+        nx_col = ld_stream_i32(a.colind + base + 32 + lane);
+        nx_val = a.vals ? ld_stream_f32(a.vals + base + 32 + lane) : 1.f;
       }
       // blocked summation: each batch of 32 nonzeros is summed into a fresh
       // partial that is then added to the row total (error ~ sqrt(32) +
       // sqrt(deg/32) roundings instead of sqrt(deg))
-      float bs[CH][VEC];
+      float blk[CH][VEC];
+      float (&bs)[CH][VEC] = BLK ? blk : acc;
+      if constexpr (BLK) {
 #pragma unroll
-      for (int c = 0; c < CH; ++c)
+        for (int c = 0; c < CH; ++c)
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) bs[c][q] = 0.f;
+          for (int q = 0; q < VEC; ++q) bs[c][q] = 0.f;
+      }
       // rounds of U nonzeros per sub-group; a runtime trip count (not an
-      // unrolled loop with early exits) keeps the loads of one round together
-      const int rounds = (n_valid + U * NSUB - 1) / (U * NSUB);
+      // unrolled loop with early exits) keeps the loads of one round
+      // together.  Only the last round of a batch can hold missing entries:
+      // the forward runs the others unpredicated (BF16 3.66 against 4.21 ms,
+      // 114.8M-edge graph, F = 256), while the fused backward keeps one
+      // predicated loop (split, it measured 10.9 against 10.0 ms in FP32).
+      if constexpr (SD) {
+        const int rounds = (n_valid + U * NSUB - 1) / (U * NSUB);
 #pragma unroll 1
-      for (int rd = 0; rd < rounds; ++rd) {
-        const int u0 = rd * U;
-        raw bv[U][CH];
-        float vv[U];
+        for (int rd = 0; rd < rounds; ++rd) {
+          const int u0 = rd * U;
+          raw bv[U][CH];
+          float vv[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int k = ((u0 + u) * NSUB + sub) & 31;
-          const int col = __shfl_sync(0xffffffffu, my_col, k);
-          const float v = __shfl_sync(0xffffffffu, my_val, k);
-          const bool ok = (u0 + u) * NSUB + sub < n_valid;
-          vv[u] = ok ? v : 0.f;
-          const size_t rowbase = (size_t)col * (size_t)a.ldb;
+          for (int u = 0; u < U; ++u) {
+            const int k = ((u0 + u) * NSUB + sub) & 31;
+            const int col = __shfl_sync(0xffffffffu, my_col, k);
+            const float v = __shfl_sync(0xffffffffu, my_val, k);
+            const bool ok = (u0 + u) * NSUB + sub < n_valid;
+            vv[u] = ok ? v : 0.f;
+            const size_t rowbase = (size_t)col * (size_t)a.ldb;
 #pragma unroll
-          for (int c = 0; c < CH; ++c) {
-            const int chunk = c * LPR + sl;
-            if (ok && chunk < a.nvec) bv[u][c] = F_::load(a.B, rowbase + (size_t)chunk * VEC);
-            else bv[u][c] = F_::zero();
+            for (int c = 0; c < CH; ++c) {
+              const int chunk = c * LPR + sl;
+              if (ok && chunk < a.nvec) bv[u][c] = F_::load(a.B, rowbase + (size_t)chunk * VEC);
+              else bv[u][c] = F_::zero();
+            }
           }
-        }
-        if constexpr (SD) {
           // each gathered chunk is widened once and feeds both the row sum
           // and the dot product with the H row (even / odd columns as the
           // two halves of FFMA2s, added at the end)
@@ -138,17 +188,19 @@ struct MergeKernel {
             sd[u] = s0 + s1;
           }
           sddmm_reduce(a, base, u0, n_valid, sub, sl, sd);
-        } else {
-#pragma unroll
-          for (int u = 0; u < U; ++u)
-#pragma unroll
-            for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
         }
+      } else {
+        const int full = n_valid / (U * NSUB);
+#pragma unroll 1
+        for (int rd = 0; rd < full; ++rd) round<false>(a, rd * U, n_valid, sub, sl, my_col, my_val, bs);
+        if (full * U * NSUB < n_valid) round<true>(a, full * U, n_valid, sub, sl, my_col, my_val, bs);
       }
+      if constexpr (BLK) {
 #pragma unroll
-      for (int c = 0; c < CH; ++c)
+        for (int c = 0; c < CH; ++c)
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) acc[c][q] += bs[c][q];
+          for (int q = 0; q < VEC; ++q) acc[c][q] += bs[c][q];
+      }
     }
     // fold the sub-groups (fixed tree order)
 #pragma unroll
