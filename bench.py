@@ -62,6 +62,25 @@ def profile_traffic():
     return None
 
 
+def gather_ceiling():
+    """Measured L2 -> SM gather ceiling (TB/s) for random 1 KB FP32 and
+    512 B BF16 feature rows of an L2-resident table, from the committed
+    summary of bin/gather_ceiling (None until one exists)."""
+    p = ROOT / "profiles" / "l2_gather_ceiling.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        best = {}
+        for r in d["results"]:
+            if r["table_rows"] == 32768:
+                k = "f32" if r["kernel"].startswith("fp32") else "bf16"
+                best[k] = max(best.get(k, 0.0), r["tbs"])
+        return best or None
+    except Exception:
+        return None
+
+
 class ClockSampler:
     """nvidia-smi sampled every 100 ms while the timed region runs."""
 
@@ -347,6 +366,18 @@ def run_ours(args):
     value = world * bytes_f32 / (ms_f32 * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = profile_traffic()
+    # the row gathers (nnz * F elements) against the measured L2 -> SM ceiling
+    ceil = gather_ceiling()
+    l2_gather = None
+    if ceil:
+        g32 = nnz * F * 4 / (ms_f32 * 1e-3) / 1e12
+        g16 = nnz * F * 2 / (ms_bf16 * 1e-3) / 1e12
+        l2_gather = {"unit": "TB/s", "f32": {"achieved": round(g32, 2), "ceiling": ceil.get("f32"),
+                                              "frac": round(g32 / ceil["f32"], 3) if ceil.get("f32") else None},
+                     "bf16": {"achieved": round(g16, 2), "ceiling": ceil.get("bf16"),
+                              "frac": round(g16 / ceil["bf16"], 3) if ceil.get("bf16") else None},
+                     "what": "row-gather bytes (nnz*F*elem) per ms vs bin/gather_ceiling on a 32 MB table "
+                             "(profiles/l2_gather_ceiling.json)"}
 
     # errors vs FP64 on sampled rows (incl. the 32 largest hubs)
     rows = sample_rows_for_error(g)
@@ -401,6 +432,7 @@ def run_ours(args):
                      "bytes_per_step": bytes_f32,
                      "per": "step = one SpMM = %d accumulating launches of k_csr_spmm_merge "
                             "(achieved and traffic both per step)" % plan32.parts},
+        "l2_gather": l2_gather,
         "fwd_bwd": {"what": "planned SpMM A H + planned fused backward (A^T dY and SDDMM(dY, H) in one pass "
                             "per row-range piece of A^T), F=256",
                     "backward_parts": {"f32": bplans[torch.float32].parts, "bf16": bplans[torch.bfloat16].parts},
@@ -434,6 +466,9 @@ def run_profile_case(args):
       eighth : same nodes (B still larger than L2), 1/8 of the degree
       fwdbwd : eighth graph, planned SpMM + planned fused backward (FP32, then
                BF16)
+      l2resident : 232,965 rows x 492 nonzeros, columns uniform over 8K / 32K /
+               128K rows (B in L2), planned FP32 and BF16 SpMM, event-timed
+               medians printed (not an ncu case)
       b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
                B2SR BMM F = 256
       bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 per tile, tcgen05
@@ -483,6 +518,38 @@ def run_profile_case(args):
                     plans[Bx.dtype].run(Bx, out=C, workspace=ws)
             out["parts"] = {"f32": plans[torch.float32].parts, "bf16": plans[torch.bfloat16].parts}
         out.update(nodes=g.nrows, nnz=g.nnz)
+    elif case == "l2resident":
+        # the bench graph's row count and mean degree with columns uniform over
+        # a table that fits L2: the planned SpMM against the gather ceiling
+        n, deg, F = 232_965, 492, 256
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(5)
+        res = []
+        for ncols in (8192, 32768, 131072):
+            ci = torch.randint(0, ncols, (n, deg), device=dev, generator=gen, dtype=torch.int32)
+            ci = torch.sort(ci, dim=1)[0].reshape(-1).contiguous()
+            rp = torch.arange(n + 1, device=dev, dtype=torch.int32) * deg
+            A = ops.CSR(rp, ci, torch.full((n * deg,), 0.5, device=dev), n, ncols)
+            C = torch.empty((n, F), device=dev)
+            ws = ops.SpmmWorkspace()
+            for dt in (torch.float32, torch.bfloat16):
+                B = G.normal(7, 7, (ncols, F), device=dev).to(dt)
+                plan = ops.SpmmPlan(A, F, dt)
+                for _ in range(3):
+                    plan.run(B, out=C, workspace=ws)
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                      for _ in range(max(args.steps, 5))]
+                for s0, s1 in ev:
+                    s0.record()
+                    plan.run(B, out=C, workspace=ws)
+                    s1.record()
+                torch.cuda.synchronize()
+                ms = sorted(s0.elapsed_time(s1) for s0, s1 in ev)[len(ev) // 2]
+                gathered = n * deg * F * (4 if dt == torch.float32 else 2)
+                res.append({"ncols": ncols, "dtype": str(dt)[6:], "parts": plan.parts, "ms": round(ms, 4),
+                            "gather_tbs": round(gathered / (ms * 1e-3) / 1e12, 3)})
+            del A, ci, rp, C
+        out["results"] = res
     elif case == "b2sr":
         g = G.flickr_like(device=dev)
         A = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
@@ -519,7 +586,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "b2sr", "bmm", "bmmtc"], default=None,
+    ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "l2resident", "b2sr", "bmm", "bmmtc"],
+                    default=None,
                     help="run a short fixed launch sequence for ncu instead of the bench")
     args = ap.parse_args()
     if args.profile_case:

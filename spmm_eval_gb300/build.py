@@ -93,8 +93,8 @@ DRIVER_NAMES = ["spmmfbf", "spmmcsr", "spmmcsr_bf16", "spmmb2sr8", "spmmb2sr16",
 
 def build_apps(verbose: bool = False) -> Path:
     """Compile apps/spmm_driver.cu into bin/spmm_driver (linked against
-    lib/libgbspmm.so and cuSPARSE, the reference's verifier) and the
-    per-kernel links."""
+    lib/libgbspmm.so and cuSPARSE, the reference's verifier), the
+    per-kernel links and bin/gather_ceiling (apps/gather_ceiling.cu)."""
     lib = build(verbose)
     BIN.mkdir(parents=True, exist_ok=True)
     exe = BIN / "spmm_driver"
@@ -108,6 +108,14 @@ def build_apps(verbose: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    # the L2 -> SM gather ceiling probe quoted beside the SpMM's gather rate
+    probe = BIN / "gather_ceiling"
+    psrc = APPS / "gather_ceiling.cu"
+    if not probe.exists() or probe.stat().st_mtime < psrc.stat().st_mtime:
+        cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", str(psrc), "-o", str(probe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gather_ceiling build failed:\n{r.stdout}\n{r.stderr}")
     for name in DRIVER_NAMES:
         link = BIN / name
         if not link.is_symlink():
