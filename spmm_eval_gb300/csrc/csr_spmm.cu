@@ -167,6 +167,8 @@ gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const in
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
                        float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base,
                        int accumulate) {
+  // the kernels address a row of B by a 32-bit byte pitch
+  GBS_REQUIRE(ldb >= 0 && ldb * 4 < (1LL << 32), "csr spmm: row stride of B too large");
   MergeArgs a;
   a.rp_base = rp_base;
   a.accumulate = accumulate;
