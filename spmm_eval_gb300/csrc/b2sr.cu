@@ -434,7 +434,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
         const int2 en = live ? list[k0 + u] : make_int2(0, 0);
         mu[u] = (unsigned)en.y;
         const bool need = (mu[u] & my_mask) != 0;
-        const size_t rb = (size_t)en.x * (size_t)a.ldb;
+        const size_t rb = (size_t)(unsigned)en.x * (unsigned)a.ldb;  // 32 x 32 -> 64-bit
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
           const int chunk = chunk0 + c * LPR + sl;
@@ -743,7 +743,7 @@ __device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br
         const bool live = k0 + u < n;
         const int2 en = live ? list[k0 + u] : make_int2(0, 0);
         mu[u] = (unsigned)en.y;
-        const uint32_t *xr = a.X + (size_t)en.x * a.W;
+        const uint32_t *xr = a.X + (size_t)(unsigned)en.x * (unsigned)a.W;
 #pragma unroll
         for (int k = 0; k < WMAX; ++k) w[u][k] = (live && k < a.W) ? __ldg(xr + k) : 0u;
       }
@@ -838,7 +838,7 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
 #pragma unroll
       for (int it = 0; it < WMAX; ++it) {
         const int u = k0 + it * EPL + my_e;
-        w[it] = (u < n && my_w < a.W) ? __ldg(a.X + (size_t)list[u].x * a.W + my_w) : 0u;
+        w[it] = (u < n && my_w < a.W) ? __ldg(a.X + (size_t)(unsigned)list[u].x * (unsigned)a.W + my_w) : 0u;
       }
       const int m = min(32, n - k0);
       deg += m;

@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256, MINB) k_sddmm(SddmmArgs a) {
 #pragma unroll
             for (int c = 0; c < CH; ++c) {
               const int chunk = c * LPR + sl;
-              if (ok && chunk < a.nvec) hv[u][c] = F_::load(a.H, (size_t)col * a.F + (size_t)chunk * VEC);
+              if (ok && chunk < a.nvec) hv[u][c] = F_::load(a.H, (size_t)(unsigned)col * (unsigned)a.F + (size_t)chunk * VEC);
               else hv[u][c] = F_::zero();
             }
           }
