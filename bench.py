@@ -462,7 +462,7 @@ def run_profile_case(args):
     """Short fixed launch sequences for ncu (2 warm-up launches, then
     `--steps` launches of each kernel, nothing else heavy):
       full   : bench graph, FP32 then BF16 planned merge-path SpMM, F = 256
-               (FP32: 4 column parts = 4 launches per step)
+               (FP32: 2 column parts = 2 launches per step)
       eighth : same nodes (B still larger than L2), 1/8 of the degree
       fwdbwd : eighth graph, planned SpMM + planned fused backward (FP32, then
                BF16)

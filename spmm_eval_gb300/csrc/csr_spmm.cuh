@@ -67,5 +67,8 @@ gbs_status partition_columns(int nrows, int ncols, int nnz, const int *rowptr, c
 // L2 or the matrix is too sparse to amortise re-reading C, else the smallest
 // power of two (<= 8) whose slices fit in half of L2.
 gbs_status auto_parts(double bbytes, long long nnz, int ncols, int *K);
+// Column parts of a forward plan: 1 under the same two conditions, else the
+// smallest power of two (2..8) whose slices fit in L2.
+gbs_status auto_parts_forward(double bbytes, long long nnz, int ncols, int *K);
 
 }  // namespace gbs
