@@ -85,6 +85,27 @@ GBS_API void gbs_host_csr_free(gbs_host_csr *csr);
 GBS_API gbs_status gbs_csr_write_bin(const char *path, const gbs_host_csr *csr);
 GBS_API gbs_status gbs_csr_read_bin(const char *path, gbs_host_csr *out);
 
+/* Host copy of a B2SR matrix (the layout of gbs_csr2b2sr's outputs):
+ * rowptr[nblockrows + 1], colind[nnzb] (tile columns ascending per block
+ * row), val[nnzb * tile] tile rows of 1 (tile 4, 8), 2 (16) or 4 (32)
+ * bytes, bit (tile - 1 - j) = column j of the tile. */
+typedef struct gbs_host_b2sr {
+  int nrows, ncols, tile, nblockrows, nnzb;
+  int *rowptr;
+  int *colind;
+  void *val;
+} gbs_host_b2sr;
+
+/* Binary B2SR cache: "GBSB2SR1", int32 nrows, ncols, tile, nblockrows, nnzb,
+ * rowptr, colind, val (host byte order), so packed tiles are kept between
+ * runs.  Both directions check the arrays (pointers from 0 to nnzb, tile
+ * columns ascending and inside the matrix, no bit past the last row or
+ * column); read fills *out (free with gbs_host_b2sr_free).  No counterpart
+ * in the reference's code path. */
+GBS_API gbs_status gbs_b2sr_write_bin(const char *path, const gbs_host_b2sr *b);
+GBS_API gbs_status gbs_b2sr_read_bin(const char *path, gbs_host_b2sr *out);
+GBS_API void gbs_host_b2sr_free(gbs_host_b2sr *b);
+
 /* ------------------------------------------------------------------------
  * CSR SpMM  C = A * B   (A: nrows x ncols CSR, B: ncols x F, C: nrows x F)
  *

@@ -31,6 +31,12 @@ st = C.c_int  # gbs_status
 pi32 = C.POINTER(C.c_int)
 psz = C.POINTER(C.c_size_t)
 
+class HostB2SR(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("tile", C.c_int), ("nblockrows", C.c_int),
+                ("nnzb", C.c_int), ("rowptr", C.POINTER(C.c_int)), ("colind", C.POINTER(C.c_int)),
+                ("val", C.c_void_p)]
+
+
 class HostCSR(C.Structure):
     _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("nnz", C.c_int),
                 ("rowptr", C.POINTER(C.c_int)), ("colind", C.POINTER(C.c_int)),
@@ -46,6 +52,9 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_host_csr_free": (None, [C.POINTER(HostCSR)]),
     "gbs_csr_write_bin": (st, [C.c_char_p, C.POINTER(HostCSR)]),
     "gbs_csr_read_bin": (st, [C.c_char_p, C.POINTER(HostCSR)]),
+    "gbs_b2sr_write_bin": (st, [C.c_char_p, C.POINTER(HostB2SR)]),
+    "gbs_b2sr_read_bin": (st, [C.c_char_p, C.POINTER(HostB2SR)]),
+    "gbs_host_b2sr_free": (None, [C.POINTER(HostB2SR)]),
     "gbs_csr_spmm_workspace_size": (st, [i32, i32, i32, i32, psz]),
     "gbs_csr_spmm_workspace_init": (st, [p, sz, p]),
     "gbs_csr_spmm": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p, sz, p]),

@@ -415,3 +415,125 @@ extern "C" gbs_status gbs_csr_read_bin(const char *path, gbs_host_csr *out) {
   }
   return GBS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Binary B2SR cache: packed tiles kept between runs.  Layout (host byte
+// order): 8-byte magic "GBSB2SR1", int32 nrows, ncols, tile, nblockrows,
+// nnzb, then rowptr[nblockrows + 1], colind[nnzb] (int32) and
+// val[nnzb * tile] in the tile's element width (1, 1, 2, 4 bytes for tiles
+// 4, 8, 16, 32).  Row r of a tile is one element whose bit (tile - 1 - j)
+// is column j of the tile, as the packers write it.
+// ---------------------------------------------------------------------------
+namespace {
+const char kB2srMagic[8] = {'G', 'B', 'S', 'B', '2', 'S', 'R', '1'};
+
+size_t tile_elem_bytes(int tile) { return tile == 32 ? 4 : (tile == 16 ? 2 : 1); }
+
+uint32_t tile_row_at(const void *val, int tile, size_t i) {
+  if (tile == 32) return static_cast<const uint32_t *>(val)[i];
+  if (tile == 16) return static_cast<const uint16_t *>(val)[i];
+  return static_cast<const uint8_t *>(val)[i];
+}
+
+// A B2SR the kernels can trust: block-row pointers from 0 to nnzb, tile
+// columns strictly ascending inside a block-row and inside the matrix, no
+// bit outside the tile's width, past the last column or on a row past the
+// last row.
+bool b2sr_consistent(const gbs_host_b2sr &b) {
+  const int T = b.tile, mb = b.nblockrows;
+  const int nbc = (b.ncols + T - 1) / T;
+  if (b.rowptr[0] != 0 || b.rowptr[mb] != b.nnzb) return false;
+  for (int i = 0; i < mb; ++i) {
+    const int s = b.rowptr[i], e = b.rowptr[i + 1];
+    if (s > e) return false;
+    for (int k = s; k < e; ++k) {
+      const int bc = b.colind[k];
+      if (bc < 0 || bc >= nbc || (k > s && bc <= b.colind[k - 1])) return false;
+      const int cols = std::min(T, b.ncols - bc * T);
+      const uint32_t allowed = (cols == 32 ? 0xffffffffu : ((1u << cols) - 1u)) << (T - cols);
+      const int rows = std::min(T, b.nrows - i * T);
+      for (int r = 0; r < T; ++r) {
+        const uint32_t w = tile_row_at(b.val, T, (size_t)k * T + r);
+        if ((w & ~allowed) != 0 || (r >= rows && w != 0)) return false;
+      }
+    }
+  }
+  return true;
+}
+}  // namespace
+
+extern "C" void gbs_host_b2sr_free(gbs_host_b2sr *b) {
+  if (!b) return;
+  std::free(b->rowptr);
+  std::free(b->colind);
+  std::free(b->val);
+  b->rowptr = nullptr;
+  b->colind = nullptr;
+  b->val = nullptr;
+}
+
+extern "C" gbs_status gbs_b2sr_write_bin(const char *path, const gbs_host_b2sr *b) {
+  clear_error();
+  GBS_REQUIRE(path && b && b->rowptr, "b2sr bin: null argument");
+  GBS_REQUIRE(b->tile == 4 || b->tile == 8 || b->tile == 16 || b->tile == 32, "b2sr bin: tile must be 4, 8, 16 or 32");
+  GBS_REQUIRE(b->nrows >= 0 && b->ncols >= 0 && b->nnzb >= 0 &&
+                  b->nblockrows == (b->nrows + b->tile - 1) / b->tile,
+              "b2sr bin: bad shape");
+  GBS_REQUIRE(b->nnzb == 0 || (b->colind && b->val), "b2sr bin: null colind / val");
+  GBS_REQUIRE(b2sr_consistent(*b), "b2sr bin: inconsistent B2SR arrays");
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(GBS_ERR_INVALID_ARG, std::string("b2sr bin: cannot create ") + path);
+  const int hdr[5] = {b->nrows, b->ncols, b->tile, b->nblockrows, b->nnzb};
+  const size_t nv = (size_t)b->nnzb * b->tile, eb = tile_elem_bytes(b->tile);
+  bool ok = std::fwrite(kB2srMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int), 5, f) == 5 &&
+            std::fwrite(b->rowptr, sizeof(int), (size_t)b->nblockrows + 1, f) == (size_t)b->nblockrows + 1 &&
+            std::fwrite(b->colind, sizeof(int), (size_t)b->nnzb, f) == (size_t)b->nnzb &&
+            std::fwrite(b->val, eb, nv, f) == nv;
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return fail(GBS_ERR_INVALID_ARG, std::string("b2sr bin: write failed: ") + path);
+  return GBS_OK;
+}
+
+extern "C" gbs_status gbs_b2sr_read_bin(const char *path, gbs_host_b2sr *out) {
+  clear_error();
+  GBS_REQUIRE(path && out, "b2sr bin: null argument");
+  std::memset(out, 0, sizeof(*out));
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(GBS_ERR_INVALID_ARG, std::string("b2sr bin: cannot open ") + path);
+  char magic[8];
+  int hdr[5];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kB2srMagic, 8) != 0 ||
+      std::fread(hdr, sizeof(int), 5, f) != 5) {
+    std::fclose(f);
+    return fail(GBS_ERR_INVALID_ARG, "b2sr bin: not a B2SR cache file");
+  }
+  const int n = hdr[0], m = hdr[1], T = hdr[2], mb = hdr[3], nnzb = hdr[4];
+  if (n < 0 || m < 0 || nnzb < 0 || !(T == 4 || T == 8 || T == 16 || T == 32) || mb != (n + T - 1) / T) {
+    std::fclose(f);
+    return fail(GBS_ERR_INVALID_ARG, "b2sr bin: corrupt header");
+  }
+  out->nrows = n;
+  out->ncols = m;
+  out->tile = T;
+  out->nblockrows = mb;
+  out->nnzb = nnzb;
+  const size_t nv = (size_t)nnzb * T, eb = tile_elem_bytes(T);
+  out->rowptr = (int *)std::malloc(sizeof(int) * ((size_t)mb + 1));
+  out->colind = (int *)std::malloc(sizeof(int) * (size_t)(nnzb > 0 ? nnzb : 1));
+  out->val = std::malloc(eb * (nv > 0 ? nv : 1));
+  if (!out->rowptr || !out->colind || !out->val) {
+    std::fclose(f);
+    gbs_host_b2sr_free(out);
+    return fail(GBS_ERR_OOM, "b2sr bin: host allocation failed");
+  }
+  bool ok = std::fread(out->rowptr, sizeof(int), (size_t)mb + 1, f) == (size_t)mb + 1 &&
+            std::fread(out->colind, sizeof(int), (size_t)nnzb, f) == (size_t)nnzb &&
+            std::fread(out->val, eb, nv, f) == nv;
+  std::fclose(f);
+  if (!ok || !b2sr_consistent(*out)) {
+    gbs_host_b2sr_free(out);
+    std::memset(out, 0, sizeof(*out));
+    return fail(GBS_ERR_INVALID_ARG, "b2sr bin: truncated or inconsistent file");
+  }
+  return GBS_OK;
+}

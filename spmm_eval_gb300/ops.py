@@ -528,3 +528,62 @@ def write_csr_bin(path, nrows: int, ncols: int, rowptr, colind, vals=None) -> No
     h.colind = ci.ctypes.data_as(C.POINTER(C.c_int))
     h.vals = va.ctypes.data_as(C.POINTER(C.c_float)) if va is not None else C.POINTER(C.c_float)()
     _lib.call("gbs_csr_write_bin", str(path).encode(), C.byref(h))
+
+
+_TILE_NP = {4: "uint8", 8: "uint8", 16: "uint16", 32: "uint32"}
+
+
+def write_b2sr_bin(path, Ab) -> None:
+    """Write a B2SR matrix as a binary cache file (gbs_b2sr_write_bin).  Ab is
+    a device B2SR or a host tuple (nrows, ncols, tile, rowptr, colind, val)
+    of numpy arrays."""
+    import numpy as np
+    if isinstance(Ab, B2SR):
+        nrows, ncols, tile = Ab.nrows, Ab.ncols, Ab.tile
+        rowptr, colind = Ab.rowptr.cpu().numpy(), Ab.colind.cpu().numpy()
+        val = Ab.val.cpu().numpy().view(_TILE_NP[tile])
+    else:
+        nrows, ncols, tile, rowptr, colind, val = Ab
+    if tile not in _TILE_NP:
+        raise ValueError("tile must be 4, 8, 16 or 32")
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colind, dtype=np.int32)
+    va = np.ascontiguousarray(val)
+    if va.dtype.itemsize != np.dtype(_TILE_NP[tile]).itemsize:
+        raise ValueError(f"tile {tile} rows are {np.dtype(_TILE_NP[tile]).itemsize}-byte words")
+    va = va.view(_TILE_NP[tile])
+    if va.size != ci.size * tile:
+        raise ValueError("val must hold nnzb * tile rows")
+    h = _lib.HostB2SR()
+    h.nrows, h.ncols, h.tile = int(nrows), int(ncols), int(tile)
+    h.nblockrows, h.nnzb = int(rp.size - 1), int(ci.size)
+    h.rowptr = rp.ctypes.data_as(C.POINTER(C.c_int))
+    h.colind = ci.ctypes.data_as(C.POINTER(C.c_int))
+    h.val = va.ctypes.data_as(C.c_void_p)
+    _lib.call("gbs_b2sr_write_bin", str(path).encode(), C.byref(h))
+
+
+def read_b2sr_bin(path) -> tuple:
+    """(nrows, ncols, tile, rowptr, colind, val) as numpy arrays from a
+    binary B2SR cache file (checked on load)."""
+    import numpy as np
+    h = _lib.HostB2SR()
+    _lib.call("gbs_b2sr_read_bin", str(path).encode(), C.byref(h))
+    try:
+        mb, nb, T = h.nblockrows, h.nnzb, h.tile
+        rowptr = np.ctypeslib.as_array(h.rowptr, (mb + 1,)).copy()
+        colind = np.ctypeslib.as_array(h.colind, (max(nb, 1),))[:nb].copy() if nb else np.zeros(0, np.int32)
+        dt = np.dtype(_TILE_NP[T])
+        raw = (C.c_char * (nb * T * dt.itemsize)).from_address(h.val) if nb else b""
+        val = np.frombuffer(bytes(raw), dtype=dt).copy() if nb else np.zeros(0, dt)
+        return h.nrows, h.ncols, T, rowptr, colind, val
+    finally:
+        _lib.load().gbs_host_b2sr_free(C.byref(h))
+
+
+def load_b2sr(path, device) -> B2SR:
+    """A B2SR cache file as a device B2SR, ready for b2sr_spmm / b2sr_bmm."""
+    nrows, ncols, tile, rowptr, colind, val = read_b2sr_bin(path)
+    t = torch.from_numpy(val.view({1: "uint8", 2: "int16", 4: "int32"}[val.dtype.itemsize]))
+    return B2SR(torch.from_numpy(rowptr).to(device), torch.from_numpy(colind).to(device), t.to(device),
+                tile, nrows, ncols)

@@ -320,3 +320,19 @@ def test_pack_sign_colud(cuda):
     X = G.normal(4, 4, (70, 100))
     got = ops.pack_sign_colud(X.to(cuda)).cpu().numpy().view(np.uint32)
     assert np.array_equal(got, oracle.pack_sign_colud(X.numpy()))
+
+
+@pytest.mark.parametrize("ts", TILES)
+def test_b2sr_cache_roundtrip_on_device(cuda, tmp_path, ts):
+    """A device B2SR written to the binary cache and loaded back gives the
+    same arrays and the same SpMM result bit for bit."""
+    _, n, m, rp, ci = GRAPHS[1]
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    f = tmp_path / f"a{ts}.b2sr"
+    ops.write_b2sr_bin(f, Ab)
+    Lb = ops.load_b2sr(f, cuda)
+    assert (Lb.nrows, Lb.ncols, Lb.tile, Lb.nnzb) == (Ab.nrows, Ab.ncols, Ab.tile, Ab.nnzb)
+    assert torch.equal(Lb.rowptr, Ab.rowptr) and torch.equal(Lb.colind, Ab.colind)
+    assert Lb.val.dtype == Ab.val.dtype and torch.equal(Lb.val, Ab.val)
+    B = G.normal(ts, 5, (m, 64), device=cuda)
+    assert torch.equal(ops.b2sr_spmm(Lb, B), ops.b2sr_spmm(Ab, B))

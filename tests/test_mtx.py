@@ -146,3 +146,59 @@ def test_csr_bin_rejects_bad_files(built_lib, tmp_path):
             ops.read_csr_bin(bad)
     with pytest.raises(_lib.GbsError, match="cannot open"):
         ops.read_csr_bin(tmp_path / "missing.bin")
+
+
+@pytest.mark.parametrize("tile", [4, 8, 16, 32])
+def test_b2sr_bin_roundtrip(built_lib, tmp_path, tile):
+    """Packed tiles (the oracle's packing of a ragged power-law graph) written
+    to the B2SR cache read back identically."""
+    import oracle
+    from spmm_eval_gb300 import graphs as G
+    g = G.chung_lu(1003, 2.0, 2.0, 60.0, 11)
+    rp, ci = g.rowptr.numpy(), g.colind.numpy()
+    brp, bci, bv = oracle.b2sr_pack(g.nrows, g.ncols, rp, ci, tile)
+    f = tmp_path / f"g{tile}.b2sr"
+    ops.write_b2sr_bin(f, (g.nrows, g.ncols, tile, brp, bci, bv))
+    n, m, T, rp2, ci2, v2 = ops.read_b2sr_bin(f)
+    assert (n, m, T) == (g.nrows, g.ncols, tile)
+    assert np.array_equal(rp2, brp) and np.array_equal(ci2, bci)
+    assert v2.dtype == bv.dtype and np.array_equal(v2, bv)
+    assert f.stat().st_size == 28 + 4 * brp.size + 4 * bci.size + bv.nbytes
+
+
+def test_b2sr_bin_rejects_bad_tiles(built_lib, tmp_path):
+    """A bit past the last column or row, a tile column out of order, a
+    wrong magic or a truncated file is an error on write or on read."""
+    # 6 x 6 matrix, tile 4: block rows {0, 1}, tile columns {0, 1}
+    rp = np.array([0, 2, 3], np.int32)
+    ci = np.array([0, 1, 1], np.int32)
+    val = np.zeros(12, np.uint8)
+    val[0] = 0b1000       # row 0, column 0
+    val[4 + 1] = 0b1100   # row 1, columns 4, 5 of tile column 1
+    val[8 + 1] = 0b0100   # row 5, column 5
+    good = (6, 6, 4, rp, ci, val)
+    f = tmp_path / "ok.b2sr"
+    ops.write_b2sr_bin(f, good)
+    assert np.array_equal(ops.read_b2sr_bin(f)[5], val)
+    bad_col = val.copy()
+    bad_col[4 + 1] = 0b1110       # column 6 does not exist
+    bad_row = val.copy()
+    bad_row[8 + 2] = 0b0100       # row 6 does not exist
+    bad_nibble = val.copy()
+    bad_nibble[0] = 0x18          # tile 4 rows use the low nibble only
+    for v, rp_, ci_ in ((bad_col, rp, ci), (bad_row, rp, ci), (bad_nibble, rp, ci),
+                        (val, rp, np.array([1, 0, 1], np.int32)), (val, np.array([0, 2, 4], np.int32), ci)):
+        with pytest.raises(_lib.GbsError, match="b2sr bin"):
+            ops.write_b2sr_bin(tmp_path / "x.b2sr", (6, 6, 4, rp_, ci_, v))
+    data = f.read_bytes()
+    for name, blob in {"magic": b"GBSB2SR2" + data[8:], "trunc": data[:-1],
+                       "header": data[:16] + np.int32(5).tobytes() + data[20:]}.items():
+        p = tmp_path / f"{name}.b2sr"
+        p.write_bytes(blob)
+        with pytest.raises(_lib.GbsError, match="b2sr bin"):
+            ops.read_b2sr_bin(p)
+    # a flipped bit past the last column inside an otherwise intact file
+    p = tmp_path / "flip.b2sr"
+    p.write_bytes(data[:-3] + bytes([data[-3] | 0b0010]) + data[-2:])
+    with pytest.raises(_lib.GbsError, match="b2sr bin"):
+        ops.read_b2sr_bin(p)
