@@ -55,3 +55,17 @@ def test_csr_spmm_rejects_bad_args_on_host(built_lib, args, frag):
 def test_empty_matrix_is_a_no_op(built_lib):
     # nrows == 0: nothing to do, no device call
     _lib.call("gbs_csr_spmm", 0, 0, 0, None, None, None, None, _lib.GBS_F32, 8, None, None, 0, None)
+
+
+def test_bench_reads_committed_measurements():
+    """bench.py's roofline inputs come from the committed ncu / probe
+    summaries: DRAM bytes per step and the L2 -> SM gather ceiling."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", HEADER.parent.parent / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    traffic = bench.profile_traffic()
+    assert traffic is not None and 1e9 < traffic < 1e11
+    ceil = bench.gather_ceiling()
+    assert ceil is not None and set(ceil) == {"f32", "bf16"}
+    assert all(10.0 < v < 40.0 for v in ceil.values())
