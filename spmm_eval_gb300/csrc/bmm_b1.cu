@@ -14,8 +14,8 @@
 //   * mma  : tensor cores, mma.sync.aligned.m16n8k256 .b1 AND-popc; XOR is
 //            recovered as popc(a) + popc(b) - 2 * and from row popcounts.
 // Of these two, popc is the faster on GB300 (8192^3: 3.6 ms against 7.5 ms
-// for the .b1 tensor path); the default is the tcgen05 kernel in bmm_tc.cu
-// (0.87 ms), which multiplies the bits expanded to FP8.
+// for the .b1 tensor path); the default is the persistent tcgen05 kernel in
+// bmm_tc.cu (0.39 ms), which multiplies the bits expanded to FP8.
 // Bit order inside a word does not matter to either (popcount of matching
 // K positions), so the reference layout is consumed as is.
 #include <cstdint>
@@ -294,10 +294,12 @@ gbs_status bmm_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, i
 
 using namespace gbs;
 
-// algo: 0 = default (the fastest measured on GB300: tcgen05 on FP8 {0,1}),
-// 1 = popc CUDA cores, 2 = tensor-core mma.sync .b1, 3 = tcgen05.  8192^3 XOR
-// counts on GB300: tcgen05 0.87 ms (1.26 P bit-ops/s, incl. the bit
-// expansion), popc 3.59 ms (306 T), mma.sync .b1 7.51 ms (146 T).
+// algo: 0 = default (the fastest measured on GB300: persistent tcgen05 on
+// FP8 {0,1}), 1 = popc CUDA cores, 2 = tensor-core mma.sync .b1, 3 = tcgen05
+// one CTA per tile, 4 = persistent tcgen05, 5 = tcgen05 cluster pairs with
+// B multicast.  8192^3 XOR counts on GB300, each incl. the bit expansion:
+// 0.39 / 0.38 / 0.60 ms for 4 / 5 / 3 (2.8 P bit-ops/s for 4), popc 3.59 ms
+// (306 T), mma.sync .b1 7.51 ms (146 T).
 extern "C" gbs_status gbs_bmm_b1(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode,
                                  int algo, int32_t *C, gbs_stream_t stream) {
   clear_error();
