@@ -25,23 +25,54 @@
 // file whose entries span lines across a cut is parsed front to back.  The
 // per-row column sorts and the final gather run on the same threads.
 #include <algorithm>
+#include <charconv>
 #include <cctype>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "common.cuh"
 
 namespace {
 
+int host_threads();
+template <typename Fn>
+void run_threads(int T, Fn f);
+
+// An array that is not value-initialised when allocated (the reader fills
+// every element before reading it).
+template <typename T>
+struct RawArray {
+  std::unique_ptr<T[]> p;
+  explicit RawArray(size_t n) : p(new T[n > 0 ? n : 1]) {}
+  T *data() { return p.get(); }
+  T &operator[](size_t i) { return p[i]; }
+  const T &operator[](size_t i) const { return p[i]; }
+};
+
+// A byte buffer that is not zero-filled when allocated.
+struct CharBuf {
+  std::unique_ptr<char[]> p;
+  size_t n = 0;
+  char *data() { return p.get(); }
+  const char *data() const { return p.get(); }
+  size_t size() const { return n; }
+  char operator[](size_t i) const { return p[i]; }
+};
+
 struct Reader {
-  std::vector<char> buf;
+  CharBuf buf;
   size_t pos = 0;
 
+  // The whole file plus a terminating NUL; files over 64 MB are read by
+  // several threads (pread of disjoint ranges).
   bool load(const char *path) {
     FILE *f = std::fopen(path, "rb");
     if (!f) return false;
@@ -52,11 +83,34 @@ struct Reader {
       std::fclose(f);
       return false;
     }
-    buf.resize((size_t)n + 1);
-    size_t got = n > 0 ? std::fread(buf.data(), 1, (size_t)n, f) : 0;
+    buf.p.reset(new char[(size_t)n + 1]);
+    size_t got = 0;
+    const int T = host_threads();
+    if (T > 1 && n > (64l << 20)) {
+      const int fd = fileno(f);
+      std::vector<size_t> part(T, 0);
+      run_threads(T, [&](int t) {
+        const size_t b = (size_t)n * t / T, e = (size_t)n * (t + 1) / T;
+        size_t done = 0;
+        while (b + done < e) {
+          const ssize_t r = pread(fd, buf.p.get() + b + done, e - b - done, (off_t)(b + done));
+          if (r <= 0) break;
+          done += (size_t)r;
+        }
+        part[t] = done;
+      });
+      // the file as far as it could be read from the start
+      for (int t = 0; t < T; ++t) {
+        const size_t b = (size_t)n * t / T, e = (size_t)n * (t + 1) / T;
+        got += part[t];
+        if (b + part[t] < e) break;
+      }
+    } else if (n > 0) {
+      got = std::fread(buf.p.get(), 1, (size_t)n, f);
+    }
     std::fclose(f);
-    buf.resize(got + 1);
-    buf[got] = '\0';
+    buf.p[got] = '\0';
+    buf.n = got + 1;
     return true;
   }
   bool eof() const { return pos + 1 >= buf.size(); }
@@ -111,6 +165,37 @@ inline const char *skip(const char *p, const char *e) {
   return p;
 }
 
+// strtol / strtof on the token at p (not whitespace), through from_chars
+// where that gives the same result: a decimal integer, or a float token
+// starting with a digit, '-' or '.' that from_chars reads up to whitespace
+// or the end of the piece.  Anything else ('+' signs, hex floats, inf / nan
+// spellings, out-of-range values) goes to strtol / strtof.  Returns the end
+// of the token, p when there is none.
+inline const char *scan_long(const char *p, const char *e, long *out) {
+  const auto r = std::from_chars(p, e, *out);
+  if (r.ec == std::errc()) return r.ptr;
+  char *end = nullptr;
+  *out = std::strtol(p, &end, 10);
+  return end;
+}
+
+inline bool ends_token(const char *q, const char *e) {
+  return q == e || *q == '\0' || std::isspace((unsigned char)*q);
+}
+
+inline const char *scan_float(const char *p, const char *e, float *out) {
+  const char c0 = *p, c1 = p + 1 < e ? p[1] : '\0';
+  const bool numeric = (c0 >= '0' && c0 <= '9') || c0 == '.' ||
+                       (c0 == '-' && ((c1 >= '0' && c1 <= '9') || c1 == '.'));
+  if (numeric) {
+    const auto r = std::from_chars(p, e, *out);
+    if (r.ec == std::errc() && ends_token(r.ptr, e)) return r.ptr;
+  }
+  char *end = nullptr;
+  *out = std::strtof(p, &end);
+  return end;
+}
+
 void parse_piece(const char *b, const char *e, bool last, int kind, long M, long N, long limit, Piece *out) {
   const char *p = b;
   out->ri.reserve((size_t)((e - b) / 8));
@@ -118,13 +203,14 @@ void parse_piece(const char *b, const char *e, bool last, int kind, long M, long
   out->v.reserve((size_t)((e - b) / 8));
   long got = 0;
   while (got < limit) {
-    char *end = nullptr;
+    const char *end = nullptr;
     p = skip(p, e);
     if (p == e) {  // piece exhausted between entries
       if (last) out->err = 1;
       return;
     }
-    const long r = std::strtol(p, &end, 10);
+    long r = 0, c = 0;
+    end = scan_long(p, e, &r);
     if (end == p) {
       out->err = 1;
       return;
@@ -135,7 +221,7 @@ void parse_piece(const char *b, const char *e, bool last, int kind, long M, long
       else out->split = true;
       return;
     }
-    const long c = std::strtol(p, &end, 10);
+    end = scan_long(p, e, &c);
     if (end == p) {
       out->err = 1;
       return;
@@ -150,9 +236,11 @@ void parse_piece(const char *b, const char *e, bool last, int kind, long M, long
         return;
       }
       if (kind == 0) {
-        val = std::strtof(p, &end);
+        end = scan_float(p, e, &val);
       } else {
-        val = (float)(int)std::strtol(p, &end, 10);
+        long iv = 0;
+        end = scan_long(p, e, &iv);
+        val = (float)(int)iv;
       }
       if (end == p) {
         out->err = 2;
@@ -231,8 +319,8 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
   if (M < 0 || N < 0 || NZ < 0 || M > 0x7fffffffL || N > 0x7fffffffL || NZ > 0x7fffffffL)
     return fail(GBS_ERR_INVALID_ARG, "mtx: size out of range");
 
-  std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
-  std::vector<float> v((size_t)NZ);
+  RawArray<int> ri((size_t)NZ), ci((size_t)NZ);
+  RawArray<float> v((size_t)NZ);
   const int T = host_threads();
   const char *body = rd.buf.data() + rd.pos, *bend = rd.buf.data() + rd.buf.size() - 1;
   bool parallel_done = false;
@@ -249,14 +337,17 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
     }
     std::vector<Piece> pc(T);
     run_threads(T, [&](int t) { parse_piece(cut[t], cut[t + 1], t == T - 1, kind, M, N, NZ, &pc[t]); });
+    // pieces in file order: where each one's entries go, up to NZ entries,
+    // the first split entry or the first bad one; then copied in parallel
     long have_n = 0;
     bool split = false;
+    int used = 0;
+    std::vector<long> off(T, 0), take(T, 0);
     for (int t = 0; t < T && have_n < NZ; ++t) {
-      const long take = std::min((long)pc[t].ri.size(), NZ - have_n);
-      std::copy(pc[t].ri.begin(), pc[t].ri.begin() + take, ri.begin() + have_n);
-      std::copy(pc[t].ci.begin(), pc[t].ci.begin() + take, ci.begin() + have_n);
-      std::copy(pc[t].v.begin(), pc[t].v.begin() + take, v.begin() + have_n);
-      have_n += take;
+      off[t] = have_n;
+      take[t] = std::min((long)pc[t].ri.size(), NZ - have_n);
+      have_n += take[t];
+      used = t + 1;
       if (have_n == NZ) break;
       if (pc[t].split) {
         split = true;
@@ -267,6 +358,11 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
       if (pc[t].err == 2) return fail(GBS_ERR_INVALID_ARG, "mtx: missing value");
       if (pc[t].err == 1) return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
     }
+    run_threads(used, [&](int t) {
+      std::copy(pc[t].ri.begin(), pc[t].ri.begin() + take[t], ri.data() + off[t]);
+      std::copy(pc[t].ci.begin(), pc[t].ci.begin() + take[t], ci.data() + off[t]);
+      std::copy(pc[t].v.begin(), pc[t].v.begin() + take[t], v.data() + off[t]);
+    });
     if (!split) {
       if (have_n < NZ) return fail(GBS_ERR_INVALID_ARG, "mtx: fewer entries than the size line states");
       parallel_done = true;
@@ -291,12 +387,46 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
     v[(size_t)e] = val;
   }
 
-  // counting sort by row (stable), then stable sort of each row by column
+  // counting sort by row (stable), then stable sort of each row by column.
+  // With several threads each counts and scatters its own range of entries
+  // (file order), the ranges placed one after another inside every row, as
+  // long as the per-thread row counters stay within a few times NZ.
   std::vector<int> rowptr((size_t)M + 1, 0);
-  for (long e = 0; e < NZ; ++e) rowptr[(size_t)ri[(size_t)e] + 1]++;
-  for (long i = 0; i < M; ++i) rowptr[(size_t)i + 1] += rowptr[(size_t)i];
-  std::vector<int> order((size_t)NZ), fill(rowptr.begin(), rowptr.end() - 1);
-  for (long e = 0; e < NZ; ++e) order[(size_t)fill[(size_t)ri[(size_t)e]]++] = (int)e;
+  RawArray<int> order((size_t)NZ);
+  const int TC = (NZ > (1l << 20) && (long long)T * (M + 1) <= 4ll * NZ) ? T : 1;
+  if (TC > 1) {
+    std::vector<std::vector<int>> cnt(TC);
+    run_threads(TC, [&](int t) {
+      cnt[t].assign((size_t)M, 0);
+      for (long e = NZ * t / TC; e < NZ * (t + 1) / TC; ++e) cnt[t][(size_t)ri[(size_t)e]]++;
+    });
+    // rows split over the threads: each row's total, and each thread's start
+    // inside the row (relative)
+    run_threads(TC, [&](int t) {
+      for (long i = M * t / TC; i < M * (t + 1) / TC; ++i) {
+        int run = 0;
+        for (int u = 0; u < TC; ++u) {
+          const int k = cnt[u][(size_t)i];
+          cnt[u][(size_t)i] = run;
+          run += k;
+        }
+        rowptr[(size_t)i + 1] = run;
+      }
+    });
+    for (long i = 0; i < M; ++i) rowptr[(size_t)i + 1] += rowptr[(size_t)i];
+    run_threads(TC, [&](int t) {
+      std::vector<int> &fill = cnt[t];
+      for (long e = NZ * t / TC; e < NZ * (t + 1) / TC; ++e) {
+        const int r = ri[(size_t)e];
+        order[(size_t)rowptr[(size_t)r] + (size_t)fill[(size_t)r]++] = (int)e;
+      }
+    });
+  } else {
+    for (long e = 0; e < NZ; ++e) rowptr[(size_t)ri[(size_t)e] + 1]++;
+    for (long i = 0; i < M; ++i) rowptr[(size_t)i + 1] += rowptr[(size_t)i];
+    std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
+    for (long e = 0; e < NZ; ++e) order[(size_t)fill[(size_t)ri[(size_t)e]]++] = (int)e;
+  }
   // per-row sorts on T threads, rows split into ranges of ~NZ / T entries
   std::vector<long> rcut(T + 1, M);
   rcut[0] = 0;
@@ -306,7 +436,7 @@ extern "C" gbs_status gbs_mtx_read(const char *path, gbs_host_csr *out) {
   run_threads(NZ > (1l << 20) ? T : 1, [&](int t) {
     const long i0 = NZ > (1l << 20) ? rcut[t] : 0, i1 = NZ > (1l << 20) ? rcut[t + 1] : M;
     for (long i = i0; i < i1; ++i)
-      std::stable_sort(order.begin() + rowptr[(size_t)i], order.begin() + rowptr[(size_t)i + 1],
+      std::stable_sort(order.data() + rowptr[(size_t)i], order.data() + rowptr[(size_t)i + 1],
                        [&](int a, int b) { return ci[(size_t)a] < ci[(size_t)b]; });
   });
 

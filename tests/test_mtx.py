@@ -202,3 +202,36 @@ def test_b2sr_bin_rejects_bad_tiles(built_lib, tmp_path):
     p.write_bytes(data[:-3] + bytes([data[-3] | 0b0010]) + data[-2:])
     with pytest.raises(_lib.GbsError, match="b2sr bin"):
         ops.read_b2sr_bin(p)
+
+
+def test_reader_float_tokens_match_strtof(built_lib, tmp_path):
+    """The threaded parser's fast number scanning gives exactly what the C
+    library's strtof (the reference's %f) gives, for every token form: signs,
+    leading dot, exponents, denormals, overflow, halfway cases, hex floats,
+    inf / nan spellings."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.strtof.restype = ctypes.c_float
+    libc.strtof.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]
+    toks = ["1.5", "-0.1", ".5", "-.5", "5.", "+2.5", "1e-40", "-1e-45", "1e-50", "3.4028236e38",
+            "-3.5e38", "1.00000005960464477539", "16777217", "0.333333343267440796", "0x1p-3",
+            "-0x1.8p1", "inf", "-Infinity", "nan", "1E+3", "007", "-0", "123456789012345678901234567890"]
+    per_tok = {t: libc.strtof(t.encode(), None) for t in toks}
+    reps = 560000 // len(toks) + 1  # an entry section over 8 MB: the threaded parser
+    n = 1000
+    rng = np.random.default_rng(5)
+    rc = rng.integers(1, n + 1, (reps * len(toks), 2))
+    lines = [f"{a} {b} {toks[i % len(toks)]}" for i, (a, b) in enumerate(rc)]
+    want = [per_tok[toks[i % len(toks)]] for i in range(len(lines))]
+    body = "\n".join(lines) + "\n"
+    assert len(body) > 8 << 20
+    f = tmp_path / "tok.mtx"
+    f.write_text("%%MatrixMarket matrix coordinate real general\n" + f"{n} {n} {len(lines)}\n" + body)
+    # the CSR orders entries by (row, col, file order); map back by that order
+    r, c = rc[:, 0] - 1, rc[:, 1] - 1
+    key = np.lexsort((np.arange(len(lines)), c, r))
+    want = np.array(want, np.float32)[key]
+    _, _, rp, ci, vv = ops.read_mtx(f)
+    assert np.array_equal(ci, c[key])
+    same = (vv.view(np.uint32) == want.view(np.uint32)) | (np.isnan(vv) & np.isnan(want))
+    assert same.all(), [toks[i % len(toks)] for i in np.nonzero(~same)[0][:5]]
