@@ -235,3 +235,22 @@ def test_reader_float_tokens_match_strtof(built_lib, tmp_path):
     assert np.array_equal(ci, c[key])
     same = (vv.view(np.uint32) == want.view(np.uint32)) | (np.isnan(vv) & np.isnan(want))
     assert same.all(), [toks[i % len(toks)] for i in np.nonzero(~same)[0][:5]]
+
+
+def test_reader_few_heavy_rows_stable(built_lib, tmp_path):
+    """Few rows and many duplicate (row, col) pairs: the threaded counting
+    sort and the per-row sorts keep file order among equal columns, as the
+    reference's stable sorts do."""
+    rng = np.random.default_rng(9)
+    nz, n, m = 1_200_000, 7, 50
+    r = rng.integers(0, n, nz)
+    c = rng.integers(0, m, nz)
+    v = (np.arange(nz) % 1000).astype(np.float32)  # distinct along file order within a pair
+    f = tmp_path / "heavy.mtx"
+    f.write_text("%%MatrixMarket matrix coordinate real general\n" + f"{n} {m} {nz}\n" +
+                 "\n".join(f"{a + 1} {b + 1} {x:g}" for a, b, x in zip(r, c, v)) + "\n")
+    assert f.stat().st_size > 8 << 20
+    key = np.lexsort((np.arange(nz), c, r))
+    _, _, rp, ci, vv = ops.read_mtx(f)
+    assert np.array_equal(rp, np.concatenate([[0], np.cumsum(np.bincount(r, minlength=n))]))
+    assert np.array_equal(ci, c[key]) and np.array_equal(vv, v[key])
