@@ -10,10 +10,15 @@ reference's reddit.mtx is not distributed).
 
 metric: SpMM achieved GB/s by the gather model -- every nonzero reads one
 whole feature row: bytes = 4(n+1) + 8 nnz + nnz*F*sizeof(B) + n*F*4 -- per
-launch, divided by the launch's CUDA-event time.  L2 is flushed (a 512 MiB
-write) before every timed step.  Extra keys: BF16-feature time, errors vs
-FP64 on sampled rows, the end-to-end number through the public API with host
-buffers, the CPU baseline, clocks.
+step, divided by the step's CUDA-event time.  L2 is flushed (a 512 MiB
+write) before every timed step.  Most of those row gathers are served by L2,
+so the line carries two rooflines: `roofline` (HBM: the step's measured DRAM
+bytes from an ncu capture over its time, against the measured copy peak) and
+`l2_gather` (the row-gather bytes over time against the L2 -> SM gather
+ceiling measured by bin/gather_ceiling in the same run).  Extra keys: BF16 and
+FP16 features (time, error), errors vs FP64 on sampled rows, forward +
+backward, the end-to-end number through the public API with host buffers,
+the other evaluation configurations (`configs`), the CPU baseline, clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -63,19 +68,22 @@ def profile_traffic():
 
 
 def gather_ceiling():
-    """Measured L2 -> SM gather ceiling (TB/s) for random 1 KB FP32 and
-    512 B BF16 feature rows of an L2-resident table, from the committed
-    summary of bin/gather_ceiling (None until one exists)."""
-    p = ROOT / "profiles" / "l2_gather_ceiling.json"
-    if not p.exists():
-        return None
+    """L2 -> SM gather ceiling (TB/s) of this GPU for random 1 KB FP32 and
+    512 B BF16 feature rows of an L2-resident 32 MB table, measured now by
+    bin/gather_ceiling (the SpMM's own access pattern and nothing else; the
+    best of its variants per row type).  None if the probe cannot run."""
+    exe = ROOT / "spmm_eval_gb300" / "bin" / "gather_ceiling"
     try:
-        d = json.loads(p.read_text())
+        if not exe.exists():
+            from spmm_eval_gb300 import build as b
+            b.build_apps()
+        r = subprocess.run([str(exe), "--json"], capture_output=True, text=True, timeout=300)
+        d = json.loads(r.stdout)
         best = {}
-        for r in d["results"]:
-            if r["table_rows"] == 32768:
-                k = "f32" if r["kernel"].startswith("fp32") else "bf16"
-                best[k] = max(best.get(k, 0.0), r["tbs"])
+        for x in d["results"]:
+            if x["table_rows"] == 32768:
+                k = "f32" if x["kernel"].startswith("fp32") else "bf16"
+                best[k] = max(best.get(k, 0.0), x["tbs"])
         return best or None
     except Exception:
         return None
@@ -169,9 +177,24 @@ def fp64_rows(g_cpu, B_cpu, rows):
 
 
 def rel_err(got, ref, mag):
+    """max and mean of |C - C64| / (|A| |B|) elementwise (the scale of the
+    rounding bound of a sum of products; |C64| itself can cancel to ~0)."""
     d = (got.double() - ref).abs()
     r = d / mag.clamp_min(1e-300)
     return float(r.max()), float(r.mean())
+
+
+def plain_rel_err(got, ref):
+    """max of the plain relative error |C - C64| / |C64| over the entries
+    with |C64| >= the RMS of C64 over the sampled rows (the stated floor:
+    below it the relative error of a cancelling sum is unbounded), and the
+    fraction of entries that pass the floor."""
+    ref = ref.double()
+    floor = float(ref.pow(2).mean().sqrt())
+    keep = ref.abs() >= floor
+    r = (got.double() - ref).abs()[keep] / ref.abs()[keep]
+    return {"max": float(r.max()) if r.numel() else 0.0, "floor": floor,
+            "entries": int(keep.sum()), "of": int(ref.numel())}
 
 
 def cpu_baseline(g_cpu, B_cpu, budget_s=10.0):
@@ -185,12 +208,13 @@ def cpu_baseline(g_cpu, B_cpu, budget_s=10.0):
     nnz = int(rp[r1])
     ci, va, Bn = g_cpu.colind.numpy(), g_cpu.vals.numpy(), B_cpu.numpy()
     threads = oracle.max_threads()
-    oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)  # warm-up
+    Cn = np.empty((r1, B_cpu.shape[1]), np.float32)
+    oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1, out=Cn)  # warm-up
     times = []
     t_end = time.perf_counter() + budget_s
     while True:
         t0 = time.perf_counter()
-        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1, out=Cn)
         times.append(time.perf_counter() - t0)
         if time.perf_counter() > t_end or len(times) >= 50:
             break
@@ -230,8 +254,10 @@ def max_over_ranks(x, world, device):
 
 
 def run_reference(args):
-    """The reference has no CPU path of its own; its semantics are timed as
-    the oracle's OpenMP FP32 CSR SpMM on the host cores (rank 0 only)."""
+    """The reference has no CPU path of its own; its semantics (FP32 CSR
+    SpMM, per-row in-order accumulation) are timed as the oracle's OpenMP
+    port on the host cores, over the whole bench graph every step (rank 0
+    only)."""
     world, rank, local = dist_setup(args)
     if rank != 0:
         return
@@ -242,64 +268,38 @@ def run_reference(args):
     g, B = make_inputs(dev)
     g_cpu, B_cpu = g.to("cpu"), B.to("cpu")
     del g, B
+    n, nnz, F = g_cpu.nrows, g_cpu.nnz, 256
+    rp, ci, va, Bn = g_cpu.rowptr.numpy(), g_cpu.colind.numpy(), g_cpu.vals.numpy(), B_cpu.numpy()
     import numpy as np
-    rp = g_cpu.rowptr.numpy()
-    r1 = int(np.searchsorted(rp, 4_000_000))
-    nnz = int(rp[r1])
-    ci, va, Bn = g_cpu.colind.numpy(), g_cpu.vals.numpy(), B_cpu.numpy()
+    Cn = np.empty((n, F), np.float32)
     for _ in range(args.warmup):
-        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+        oracle.csr_spmm_f32(rp, ci, va, Bn, out=Cn)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.csr_spmm_f32(rp, ci, va, Bn, 0, r1)
+        oracle.csr_spmm_f32(rp, ci, va, Bn, out=Cn)
         times.append(time.perf_counter() - t0)
     t = sum(times) / len(times)
-    gb = gather_bytes(r1, nnz, 256, 4) / 1e9
-    value = gb / t
+    value = gather_bytes(n, nnz, F, 4) / 1e9 / t
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nodes": g_cpu.nrows, "nnz": g_cpu.nnz, "F": 256,
-                   "sample_rows": r1, "sample_nnz": nnz},
+        "config": {"workload": WORKLOAD, "nodes": n, "nnz": nnz, "F": F},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": oracle.max_threads(),
                          "kind": "port",
-                         "sample": f"rows [0,{r1}) = {nnz} nonzeros per step, F=256 FP32"},
+                         "sample": f"the whole graph ({nnz} nonzeros) per step, F=256 FP32"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+def event_timer(dev, stream, flush):
+    """timed(fn, steps, tag) -> per-step CUDA-event times (ms) on `stream`,
+    with L2 flushed (a 512 MiB write) before every step."""
     import torch
-    from spmm_eval_gb300 import ops
-    world, rank, local = dist_setup(args)
-    dev = torch.device(f"cuda:{local}")
-    torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream(dev)
-
-    g, B = make_inputs(dev)
-    n, nnz, F = g.nrows, g.nnz, 256
-    A = ops.CSR(g.rowptr, g.colind, g.vals, n, n)
-    Bh = B.to(torch.bfloat16)
-    C = torch.empty((n, F), dtype=torch.float32, device=dev)
-    Ch = torch.empty_like(C)
-    ws = ops.SpmmWorkspace()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-
-    # column-partitioned plans (built once, like cuSPARSE's SpMM preprocessing;
-    # the library picks the number of column ranges from B's size against L2)
-    plan32 = ops.SpmmPlan(A, F, torch.float32)
-    plan16 = ops.SpmmPlan(A, F, torch.bfloat16)
-
-    def step_f32():
-        plan32.run(B, out=C, workspace=ws)
-
-    def step_bf16():
-        plan16.run(Bh, out=Ch, workspace=ws)
 
     def timed(fn, steps, tag):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -313,10 +313,165 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
         torch.cuda.nvtx.range_pop()
         return [s.elapsed_time(e) for s, e in evs]
+    return timed
+
+
+def mean_ms(timed, fn, steps, tag, warm=2):
+    for _ in range(warm):
+        fn()
+    t = timed(fn, steps, tag)
+    return sum(t) / len(t)
+
+
+def other_configs(dev, timed, reps):
+    """The other evaluation configurations, event-timed (L2 flushed before
+    each rep): the 4096-row uniform matrix (F = 32); the 89,250-node
+    flickr-shaped graph (CSR SpMM at F = 32..256, CSR -> B2SR packing and
+    B2SR x FP32 SpMM at tiles 4/8/16/32, B2SR x bits BMM at F = 32..1024); the
+    8192^3-bit binary GEMM; one GCN layer Y = A (X W) forward + backward on
+    the normalised flickr-shaped graph (X 89,250 x 512, W 512 x 128)."""
+    import torch
+    from spmm_eval_gb300 import graphs as G
+    from spmm_eval_gb300 import ops
+    out = {}
+    ws = ops.SpmmWorkspace()
+
+    # uniform 4096 x 4096, 16 columns per row, values U[-1, 1], F = 32
+    g = G.uniform_rows(4096, 16, device=dev)
+    A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
+    B = G.normal(0x5EED + 1, 3, (4096, 32), device=dev)
+    C = torch.empty((4096, 32), device=dev)
+    ms = mean_ms(timed, lambda: ops.csr_spmm(A, B, out=C, workspace=ws), reps, "uniform4096")
+    out["uniform4096_f32_f32"] = {"ms": round(ms, 4),
+                                  "gbs_gather_model": round(gather_bytes(4096, g.nnz, 32, 4) / (ms * 1e-3) / 1e9, 1)}
+
+    # flickr-shaped graph
+    g = G.flickr_like(device=dev)
+    n, nnz = g.nrows, g.nnz
+    A = ops.CSR(g.rowptr, g.colind, g.vals, n, n)
+    Ap = ops.CSR(g.rowptr, g.colind, None, n, n)
+    fl = {"nodes": n, "nnz": nnz, "csr_spmm_f32": {}, "pack_ms": {}, "b2sr_spmm_f256_ms": {},
+          "fbf_tile4_ms": {}, "bmm_ms": {}}
+    Ab4 = ops.csr2b2sr(Ap, 4)
+    for F in (32, 64, 128, 256):
+        B = G.normal(F, 3, (n, F), device=dev)
+        C = torch.empty((n, F), device=dev)
+        ms = mean_ms(timed, lambda: ops.csr_spmm(A, B, out=C, workspace=ws), reps, f"flickr_csr_{F}")
+        fl["csr_spmm_f32"][str(F)] = {"ms": round(ms, 4),
+                                      "gbs_gather_model": round(gather_bytes(n, nnz, F, 4) / (ms * 1e-3) / 1e9, 1)}
+        fl["fbf_tile4_ms"][str(F)] = round(mean_ms(timed, lambda: ops.b2sr_spmm(Ab4, B, out=C), reps,
+                                                   f"flickr_fbf_{F}"), 4)
+    B = G.normal(256, 3, (n, 256), device=dev)
+    C = torch.empty((n, 256), device=dev)
+    for ts in (4, 8, 16, 32):
+        holder = {}
+
+        def pack():
+            holder["Ab"] = ops.csr2b2sr(Ap, ts)
+        fl["pack_ms"][str(ts)] = round(mean_ms(timed, pack, reps, f"flickr_pack_{ts}"), 4)
+        Ab = holder["Ab"]
+        fl["b2sr_spmm_f256_ms"][str(ts)] = round(mean_ms(timed, lambda: ops.b2sr_spmm(Ab, B, out=C), reps,
+                                                         f"flickr_b2sr_{ts}"), 4)
+        fl.setdefault("nnzb", {})[str(ts)] = Ab.nnzb
+        bm = {}
+        for F in (32, 64, 128, 256, 512, 1024):
+            X = G.normal(F + 1, 8, (n, F), device=dev)
+            Xw = ops.pack_sign_rows(X)
+            bm[str(F)] = round(mean_ms(timed, lambda: ops.b2sr_bmm(Ab, Xw, F), reps, f"flickr_bmm_{ts}_{F}"), 4)
+        fl["bmm_ms"][str(ts)] = bm
+    out["flickr_like"] = fl
+
+    # binary GEMM 8192 x 8192 x 8192 bits (default: persistent tcgen05)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(8192)
+    Aw = torch.randint(-2 ** 31, 2 ** 31 - 1, (256, 8192), dtype=torch.int32, device=dev, generator=gen)
+    Bw = torch.randint(-2 ** 31, 2 ** 31 - 1, (256, 8192), dtype=torch.int32, device=dev, generator=gen)
+    Co = torch.empty((8192, 8192), dtype=torch.int32, device=dev)
+    ms = mean_ms(timed, lambda: ops.bmm_b1(Aw, Bw, ops.BMM_XOR, out=Co), reps, "bmm8192")
+    ms_popc = mean_ms(timed, lambda: ops.bmm_b1(Aw, Bw, ops.BMM_XOR, ops.BMM_ALGO_POPC, out=Co), reps,
+                      "bmm8192_popc")
+    out["bmm_8192"] = {"ms": round(ms, 4), "pbitops": round(2 * 8192 ** 3 / (ms * 1e-3) / 1e15, 3),
+                       "popc_ms": round(ms_popc, 4), "timeouts": ops.bmm_tc_timeouts()}
+    del Aw, Bw, Co
+
+    # GCN layer on the normalised flickr-shaped graph
+    gn = G.gcn_normalize(g)
+    An = ops.CSR(gn.rowptr, gn.colind, gn.vals, n, n)
+    T = ops.CSRTranspose(ops.CSR(gn.rowptr, gn.colind, None, n, n))
+    tv = T.values(gn.vals)
+    X = G.normal(51, 1, (n, 512), device=dev)
+    lim = (6.0 / (512 + 128)) ** 0.5
+    W = ((2 * G.uniform01(52, 0, torch.arange(512 * 128, device=dev)).reshape(512, 128) - 1) * lim).float()
+    Gr = G.normal(53, 2, (n, 128), device=dev)
+    gcn = {}
+    for dt in (torch.float32, torch.bfloat16):
+        pf = ops.SpmmPlan(An, 128, dt)
+        pb = ops.BackwardPlan(T, tv, 128, dt)
+        Y = torch.empty((n, 128), device=dev)
+        dH = torch.empty((n, 128), device=dev)
+        dv = torch.empty_like(gn.vals)
+        Gx = Gr.to(dt)
+
+        def layer():
+            H = (X @ W).to(dt)            # dense X W (cuBLAS, in the harness)
+            pf.run(H, out=Y, workspace=ws)  # Y = A H
+            pb.run(Gx, H, dB=dH, dvals=dv, workspace=ws)  # dH = A^T G, dvals = SDDMM(G, H)
+            return H
+
+        def sparse_only(H):
+            pf.run(H, out=Y, workspace=ws)
+            pb.run(Gx, H, dB=dH, dvals=dv, workspace=ws)
+        H = layer()
+        gcn[str(dt)[6:]] = {"layer_ms": round(mean_ms(timed, layer, reps, "gcn_layer"), 4),
+                            "sparse_ms": round(mean_ms(timed, lambda: sparse_only(H), reps, "gcn_sparse"), 4)}
+    gcn["what"] = ("forward Y = A (X W) + backward dH = A^T G and dvals = SDDMM(G, X W); X W by torch "
+                   "matmul (FP32); sparse_ms = the library's planned SpMM + planned fused backward only")
+    out["gcn_layer_flickr"] = gcn
+    return out
+
+
+def run_ours(args):
+    import torch
+    from spmm_eval_gb300 import ops
+    world, rank, local = dist_setup(args)
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    # the L2 -> SM gather ceiling of this GPU, measured before anything else
+    ceil = gather_ceiling()
+
+    g, B = make_inputs(dev)
+    n, nnz, F = g.nrows, g.nnz, 256
+    A = ops.CSR(g.rowptr, g.colind, g.vals, n, n)
+    Bh = B.to(torch.bfloat16)
+    Bf = B.to(torch.float16)
+    C = torch.empty((n, F), dtype=torch.float32, device=dev)
+    Ch = torch.empty_like(C)
+    Cf = torch.empty_like(C)
+    ws = ops.SpmmWorkspace()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    timed = event_timer(dev, stream, flush)
+
+    # column-partitioned plans (built once, like cuSPARSE's SpMM preprocessing;
+    # the library picks the number of column ranges from B's size against L2)
+    plan32 = ops.SpmmPlan(A, F, torch.float32)
+    plan16 = ops.SpmmPlan(A, F, torch.bfloat16)
+    planh = ops.SpmmPlan(A, F, torch.float16)
+
+    def step_f32():
+        plan32.run(B, out=C, workspace=ws)
+
+    def step_bf16():
+        plan16.run(Bh, out=Ch, workspace=ws)
+
+    def step_f16():
+        planh.run(Bf, out=Cf, workspace=ws)
 
     for _ in range(max(3, args.warmup)):
         step_f32()
         step_bf16()
+        step_f16()
     torch.cuda.synchronize(dev)
 
     barrier(world)
@@ -331,6 +486,7 @@ def run_ours(args):
     ms_f32 = sum(ms) / len(ms)
     ms_f32 = max_over_ranks(ms_f32, world, dev)
     ms_bf16 = sum(timed(step_bf16, args.steps, "timed_bf16")) / args.steps
+    ms_f16 = sum(timed(step_f16, args.steps, "timed_f16")) / args.steps
 
     # forward + backward of Y = A H: fwd SpMM, bwd A^T dY (cached transpose)
     # and SDDMM for d(values); FP32 vs BF16 features (H, dY), FP32 accumulate
@@ -340,7 +496,6 @@ def run_ours(args):
     Gh = Gd.to(torch.bfloat16)
     dH = torch.empty_like(C)
     dvals = torch.empty_like(g.vals)
-    Apat = ops.CSR(g.rowptr, g.colind, None, n, n)
 
     # planned fused backward: A^T dY and SDDMM(dY, H) in one pass over each
     # row-range piece of A^T (pieces chosen so the dY slice fits in L2)
@@ -359,15 +514,14 @@ def run_ours(args):
     fb_steps = max(3, min(args.steps, 20))
     ms_fb32 = sum(timed(lambda: fwd_bwd(B, Gd, C), fb_steps, "timed_fwdbwd_f32")) / fb_steps
     ms_fb16 = sum(timed(lambda: fwd_bwd(Bh, Gh, Ch), fb_steps, "timed_fwdbwd_bf16")) / fb_steps
-    del Gd, Gh
+    del Gd, Gh, T
 
     bytes_f32 = gather_bytes(n, nnz, F, 4)
     bytes_bf16 = gather_bytes(n, nnz, F, 2)
     value = world * bytes_f32 / (ms_f32 * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = profile_traffic()
-    # the row gathers (nnz * F elements) against the measured L2 -> SM ceiling
-    ceil = gather_ceiling()
+    # the row gathers (nnz * F elements) against the L2 -> SM ceiling measured above
     l2_gather = None
     if ceil:
         g32 = nnz * F * 4 / (ms_f32 * 1e-3) / 1e12
@@ -376,16 +530,27 @@ def run_ours(args):
                                               "frac": round(g32 / ceil["f32"], 3) if ceil.get("f32") else None},
                      "bf16": {"achieved": round(g16, 2), "ceiling": ceil.get("bf16"),
                               "frac": round(g16 / ceil["bf16"], 3) if ceil.get("bf16") else None},
-                     "what": "row-gather bytes (nnz*F*elem) per ms vs bin/gather_ceiling on a 32 MB table "
-                             "(profiles/l2_gather_ceiling.json)"}
+                     "what": "row-gather bytes (nnz*F*elem) per second vs the ceiling bin/gather_ceiling "
+                             "measured in this run (random rows of an L2-resident 32 MB table)"}
 
     # errors vs FP64 on sampled rows (incl. the 32 largest hubs)
     rows = sample_rows_for_error(g)
     g_cpu = g.to("cpu")
     B_cpu = B.to("cpu")
     ref, mag = fp64_rows(g_cpu, B_cpu, rows)
-    e32 = rel_err(C[rows.to(dev)].cpu(), ref, mag)
-    e16 = rel_err(Ch[rows.to(dev)].cpu(), ref, mag)
+    rd = rows.to(dev)
+    errs = {}
+    for tag, Cx in (("f32", C), ("bf16_features", Ch), ("fp16_features", Cf)):
+        got = Cx[rd].cpu()
+        mx, mean = rel_err(got, ref, mag)
+        errs[tag] = {"max": mx, "mean": mean, "plain": plain_rel_err(got, ref)}
+    del Ch, Cf, Bh, Bf
+
+    # the other configurations
+    others = None
+    if not args.no_configs:
+        others = other_configs(dev, timed, max(3, min(args.steps, 5)))
+        torch.cuda.empty_cache()
 
     # end to end through the public host-buffer entry point (gbs_csr_spmm_host):
     # pinned host A and B in, host C out, copies overlapped with the kernels
@@ -416,7 +581,10 @@ def run_ours(args):
 
     if rank != 0:
         return
-    achieved = bytes_f32 / (ms_f32 * 1e-3) / 1e9
+    # HBM roofline of the step: the DRAM bytes ncu measured for one step of
+    # these launches, over this run's step time (the gather-model bytes would
+    # read ~3x the copy peak, since L2 serves most row gathers)
+    hbm_achieved = traffic / (ms_f32 * 1e-3) / 1e9 if traffic else None
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_f32, 4),
@@ -425,13 +593,15 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "nodes": n, "nnz": nnz, "F": F,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every timed step (512 MiB write)"},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+        "roofline": {"bound": "hbm", "achieved": round(hbm_achieved, 1) if hbm_achieved else None,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(hbm_achieved / peak, 4) if hbm_achieved else None,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "bytes_model": "gather: 4(n+1)+8nnz+nnz*F*4+n*F*4 per SpMM",
-                     "bytes_per_step": bytes_f32,
-                     "per": "step = one SpMM = %d accumulating launches of k_csr_spmm_merge "
-                            "(achieved and traffic both per step)" % plan32.parts},
+                     "achieved_is": "measured DRAM bytes per step (ncu dram__bytes_read.sum + "
+                                    "dram__bytes_write.sum, profiles/csr_spmm_plan_reddit_f256.md) / ms_per_step",
+                     "gather_model_bytes_per_step": bytes_f32,
+                     "per": "step = one SpMM = %d accumulating launches of k_csr_spmm_merge" % plan32.parts,
+                     "binding_roofline": "l2_gather"},
         "l2_gather": l2_gather,
         "fwd_bwd": {"what": "planned SpMM A H + planned fused backward (A^T dY and SDDMM(dY, H) in one pass "
                             "per row-range piece of A^T), F=256",
@@ -441,16 +611,21 @@ def run_ours(args):
         "bf16": {"ms_per_step": round(ms_bf16, 4),
                  "gbs_gather_model": round(bytes_bf16 / (ms_bf16 * 1e-3) / 1e9, 1),
                  "speedup_vs_f32": round(ms_f32 / ms_bf16, 3)},
+        "fp16": {"ms_per_step": round(ms_f16, 4),
+                 "gbs_gather_model": round(bytes_bf16 / (ms_f16 * 1e-3) / 1e9, 1),
+                 "speedup_vs_f32": round(ms_f32 / ms_f16, 3)},
         "error_vs_fp64": {"rows_sampled": int(rows.numel()),
-                          "scale": "|C-C64| / (|A| |B|) elementwise",
-                          "f32": {"max": e32[0], "mean": e32[1]},
-                          "bf16_features": {"max": e16[0], "mean": e16[1]}},
+                          "scale": "max/mean: |C-C64| / (|A| |B|) elementwise; plain: |C-C64| / |C64| over "
+                                   "entries with |C64| >= floor = RMS of C64 on the sampled rows",
+                          **errs},
         "e2e": {"value": round(world * bytes_f32 / (ms_e2e * 1e-3) / 1e9, 2), "unit": "GB/s",
                 "ms_per_step": round(ms_e2e, 3), "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "gbs_csr_spmm_host (pinned host A, B -> host C)",
                 "max_rel_err": e2e_err},
         "gpu_launches": args.steps * plan32.parts,
-        "plan": {"f32_column_parts": plan32.parts, "bf16_column_parts": plan16.parts},
+        "plan": {"f32_column_parts": plan32.parts, "bf16_column_parts": plan16.parts,
+                 "fp16_column_parts": planh.parts},
+        "configs": others,
         "timed_region_wall_s": round(wall, 3),
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -586,6 +761,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other evaluation configurations")
     ap.add_argument("--profile-case", choices=["full", "eighth", "fwdbwd", "l2resident", "b2sr", "bmm", "bmmtc"],
                     default=None,
                     help="run a short fixed launch sequence for ncu instead of the bench")

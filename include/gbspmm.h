@@ -173,6 +173,34 @@ GBS_API gbs_status gbs_csr_spmm_planned(const gbs_csr_spmm_plan *plan, const voi
                                 size_t workspace_bytes, gbs_stream_t stream);
 GBS_API gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *plan);
 
+/* Degree-normalised binary A: C[r] = rowscale[r] * sum over the stored
+ * entries (r, c) of colscale[c] * B[c] -- the GCN propagation
+ * D^-1/2 A D^-1/2 B with the normalisation folded into the kernel instead of
+ * a value array (no 4-byte value per nonzero is streamed; each nonzero reads
+ * its column's scale, an array of ncols floats that stays in cache, and each
+ * row is scaled once in the epilogue).  A's values are not used: every
+ * stored entry counts as 1, as in the reference's binary B2SR path
+ * (spmm.cu:877-956), and the scaling is that of the normalised graphs the
+ * evaluation runs on.  rowscale / colscale may be NULL (= 1).  Workspace,
+ * schedule and feature types as gbs_csr_spmm. */
+GBS_API gbs_status gbs_csr_spmm_scaled(int nrows, int ncols, int nnz, const int *d_rowptr,
+                               const int *d_colind, const float *d_rowscale,
+                               const float *d_colscale, const void *d_B, gbs_dtype btype,
+                               int F, float *d_C, void *d_workspace, size_t workspace_bytes,
+                               gbs_stream_t stream);
+/* The column-partitioned plan of gbs_csr_spmm_scaled (run with
+ * gbs_csr_spmm_planned); the plan keeps copies of the scales. */
+GBS_API gbs_status gbs_csr_spmm_plan_create_scaled(int nrows, int ncols, int nnz,
+                                           const int *d_rowptr, const int *d_colind,
+                                           const float *d_rowscale, const float *d_colscale,
+                                           gbs_dtype btype, int F, int parts,
+                                           gbs_stream_t stream, gbs_csr_spmm_plan **out);
+/* out[r] = 1 / sqrt(deg(r)), deg = rowptr[r+1] - rowptr[r], computed in
+ * FP64 on the device and rounded once to FP32 (0 for an empty row): the
+ * D^-1/2 factors of a symmetric adjacency. */
+GBS_API gbs_status gbs_degree_rsqrt(int nrows, const int *d_rowptr, float *d_out,
+                            gbs_stream_t stream);
+
 /* Host-buffer form for callers that hold A, B and C in host memory, as the
  * reference's evalCSRSpmmFloatCuSPARSE does (test_spmm_full.cu:212-342):
  * copies in, C = A * B, copies out, and returns when h_C is filled.  A is
@@ -371,14 +399,12 @@ GBS_API gbs_status gbs_pack_sign_colud(const float *d_A, int H, int W, uint32_t 
  * AND-popc (XOR from row popcounts), 3 = tcgen05 tensor cores on the bits
  * expanded to FP8 {0, 1}, one CTA per 128 x 256 tile, 4 = the same MMAs in
  * a persistent warp-specialised kernel (one CTA per SM, two TMEM
- * accumulators so a tile's epilogue overlaps the next tile's MMAs), 5 = its
- * cluster-pair form (two CTAs share each B block through TMA multicast).
- * 3, 4 and 5 are exact and allocate (M+N)*K bytes of temporaries,
- * stream-ordered.
- * 8192^3 XOR on GB300: 0.39 / 0.38 / 0.60 / 3.59 / 7.51 ms for 4 / 5 / 3 / 1 / 2. */
+ * accumulators so a tile's epilogue overlaps the next tile's MMAs).  3 and
+ * 4 are exact and allocate (M+N)*K bytes of temporaries, stream-ordered.
+ * 8192^3 XOR on GB300: 0.39 / 0.60 / 3.59 / 7.51 ms for 4 / 3 / 1 / 2. */
 GBS_API gbs_status gbs_bmm_b1(const uint32_t *d_A, const uint32_t *d_B, int M, int N,
                       int Kw, int mode, int algo, int32_t *d_C, gbs_stream_t stream);
-/* Number of bounded mbarrier waits that ran out in algo-3/4/5 launches of this
+/* Number of bounded mbarrier waits that ran out in algo-3/4 launches of this
  * process (0 in normal operation; each timeout also skips that tile's
  * stores).  Synchronises with the device. */
 GBS_API gbs_status gbs_bmm_tc_timeouts(int *count);
@@ -404,11 +430,14 @@ GBS_API gbs_status gbs_bmm32s_bin(const uint32_t *d_A, const uint32_t *d_B, uint
  * the device).  Same arguments and result as gbs_csr_spmm minus the
  * workspace: the kernel's scratch is a fixed 8 MiB array compiled into the
  * library, held on every GPU that loads the library until the process exits.
- * Shapes whose scratch would not fit are rejected with GBS_ERR_INVALID_ARG.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture starts.  All calls share the array:
- * calls that can overlap on the GPU race and must be serialised by the
- * caller. */
+ * The warp count is reduced until the scratch fits, so rows wider than about
+ * 128 FP32 columns run with fewer warps than a full wave (slower, same
+ * result); widths gbs_csr_spmm does not support fail with
+ * GBS_ERR_UNSUPPORTED as there.  The device address of the array is looked
+ * up on every call; the first call in a CUDA context loads the library's
+ * device code, so make that first call before any stream capture starts.
+ * All calls share the array: calls that can overlap on the GPU race and
+ * must be serialised by the caller. */
 GBS_API gbs_status gbs_csr_spmm_noalloc(int nrows, int ncols, int nnz,
                                 const int *d_rowptr, const int *d_colind,
                                 const float *d_vals, const void *d_B,

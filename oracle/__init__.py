@@ -22,11 +22,13 @@ _lock = threading.Lock()
 _lib = None
 
 
-def build(ref: bool = False) -> None:
-    """make the oracle (and, if ref, the reference readMtx harness)."""
+def build(ref_dir: str | None = None) -> None:
+    """make the oracle; with ref_dir (a reference checkout), also the
+    reference-built checkers in _ref/ (the readMtx harness and the fatbin of
+    the reference's CUDA kernels)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+    if ref_dir:
+        subprocess.run(["make", "-s", "-C", str(HERE), f"REF={ref_dir}", "ref", "refkern"], check=True)
 
 
 def lib() -> C.CDLL:
@@ -72,13 +74,18 @@ def csr_spmm_f64(rowptr, colind, vals, B, rows=None, with_mag=True):
     return Cout, M
 
 
-def csr_spmm_f32(rowptr, colind, vals, B, r0=0, r1=None, nthreads=0):
+def csr_spmm_f32(rowptr, colind, vals, B, r0=0, r1=None, nthreads=0, out=None):
+    """FP32 C[r0:r1] = A[r0:r1] @ B, OpenMP over rows (out: optional
+    preallocated (r1 - r0, F) float32 C-contiguous array)."""
     rowptr, colind, B = _i32(rowptr), _i32(colind), _f32(B)
     vals = None if vals is None else _f32(vals)
     n = rowptr.size - 1
     r1 = n if r1 is None else r1
     F = B.shape[1]
-    out = np.empty((r1 - r0, F), np.float32)
+    if out is None:
+        out = np.empty((r1 - r0, F), np.float32)
+    elif out.shape != (r1 - r0, F) or out.dtype != np.float32 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float32 array of shape (r1 - r0, F)")
     lib().orc_csr_spmm_f32(C.c_int(r0), C.c_int(r1), _p(rowptr), _p(colind), _p(vals), _p(B),
                            C.c_int(F), _p(out), C.c_int(nthreads))
     return out

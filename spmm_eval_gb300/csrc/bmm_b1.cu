@@ -248,7 +248,7 @@ __global__ void k_sign_words(const int32_t *__restrict__ X, int m, int k, int nb
   }
 }
 
-// form: 0 = one CTA per tile, 1 = persistent, 2 = persistent CTA pairs
+// form: 0 = one CTA per tile, 1 = persistent
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
                       int ldc, cudaStream_t s, int form);
 gbs_status bmm_tc_error_count(int *out);
@@ -257,7 +257,6 @@ gbs_status bmm_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, i
                    int32_t *C, float *Cf, int ldc, cudaStream_t s) {
   if (algo == 0 || algo == 4) return bmm_tc_run(A, B, M, N, Kw, mode, C, Cf, ldc, s, 1);
   if (algo == 3) return bmm_tc_run(A, B, M, N, Kw, mode, C, Cf, ldc, s, 0);
-  if (algo == 5) return bmm_tc_run(A, B, M, N, Kw, mode, C, Cf, ldc, s, 2);
   GBS_REQUIRE(M % 4 == 0 && N % 4 == 0, "bmm: M and N must be multiples of 4");
   GBS_REQUIRE((reinterpret_cast<uintptr_t>(A) & 15u) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0,
               "bmm: A and B must be 16-byte aligned");
@@ -296,16 +295,16 @@ using namespace gbs;
 
 // algo: 0 = default (the fastest measured on GB300: persistent tcgen05 on
 // FP8 {0,1}), 1 = popc CUDA cores, 2 = tensor-core mma.sync .b1, 3 = tcgen05
-// one CTA per tile, 4 = persistent tcgen05, 5 = tcgen05 cluster pairs with
-// B multicast.  8192^3 XOR counts on GB300, each incl. the bit expansion:
-// 0.39 / 0.38 / 0.60 ms for 4 / 5 / 3 (2.8 P bit-ops/s for 4), popc 3.59 ms
+// one CTA per tile, 4 = persistent tcgen05.  8192^3 XOR counts on GB300,
+// each incl. the bit expansion: 0.39 / 0.60 ms for 4 / 3 (2.8 P bit-ops/s
+// for 4), popc 3.59 ms
 // (306 T), mma.sync .b1 7.51 ms (146 T).
 extern "C" gbs_status gbs_bmm_b1(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode,
                                  int algo, int32_t *C, gbs_stream_t stream) {
   clear_error();
   GBS_REQUIRE(M >= 0 && N >= 0 && Kw >= 1, "bmm: bad sizes");
   GBS_REQUIRE(mode >= 0 && mode <= 2, "bmm: mode must be 0 (xor), 1 (and) or 2 (32*Kw - 2*xor)");
-  GBS_REQUIRE(algo >= 0 && algo <= 5, "bmm: algo must be 0..5");
+  GBS_REQUIRE(algo >= 0 && algo <= 4, "bmm: algo must be 0..4");
   if (M == 0 || N == 0) return GBS_OK;
   GBS_REQUIRE(A && B && C, "bmm: null pointer");
   return bmm_run(A, B, M, N, Kw, mode, algo, C, nullptr, N, (cudaStream_t)stream);

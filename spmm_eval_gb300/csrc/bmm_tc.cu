@@ -9,7 +9,7 @@
 // the FP32 accumulation is exact; XOR counts come from row popcounts as
 // popc(a) + popc(b) - 2 and(a, b).
 //
-// Three launch forms share the tile machinery.  k_bmm_tc: one 128-thread
+// Two launch forms share the tile machinery.  k_bmm_tc: one 128-thread
 // CTA per 128 x 256 output tile.  Thread 0 of warp 0 streams 128-byte K
 // slices of A (128 rows) and B (256 rows) into a 4-stage shared-memory ring
 // with TMA (cp.async.bulk.tensor, 128B swizzle, mbarrier complete_tx);
@@ -18,8 +18,7 @@
 // after the last slice all four warps read their 32 TMEM lanes (= output
 // rows) with tcgen05.ld and write int32 C.  k_bmm_tc_persist (the default):
 // the same roles in a persistent warp-specialised CTA per SM with two TMEM
-// accumulators.  k_bmm_tc_pair: the persistent kernel on CTA pairs sharing
-// B blocks by TMA multicast.  Every mbarrier wait is bounded: on timeout the
+// accumulators.  Every mbarrier wait is bounded: on timeout the
 // kernel records an error flag, skips the remaining work, frees its tensor
 // memory and returns.
 #include <cuda.h>
@@ -406,176 +405,6 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
-// Cluster-pair version of the persistent kernel: the two CTAs of a cluster
-// compute the two 128 x 256 tiles of a 256 x 256 pair tile that share their
-// B block.  Each CTA loads its own A slice and half of the B slice, the B
-// half multicast into both CTAs' shared memory (TMA .multicast::cluster), so
-// an SM pulls 32 KiB from L2 per K step instead of 48 KiB.  A ring slot may
-// be refilled only when both CTAs' MMAs have read it: every MMA batch
-// commits to the slot's empty barrier in both CTAs (count 2).  Full barriers
-// expect 48 KiB: the own A, the own B half and the peer's.  A cluster
-// barrier after the barrier set-up (before any multicast) and one before
-// exit (after each producer has seen its last copies land and its empty
-// barriers receive both CTAs' last commits) keep every remote write and
-// arrive inside the lifetime of the CTA it targets.  All waits are bounded.
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(mask)
-      : "memory");
-}
-
-__global__ void __launch_bounds__(192, 1)
-    k_bmm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh, BmmTcArgs a) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t *sA = base;
-  uint8_t *sB = base + TC_STAGES * TC_A_BYTES;
-  uint64_t *full = reinterpret_cast<uint64_t *>(sB + TC_STAGES * TC_B_BYTES);
-  uint64_t *empty = full + TC_STAGES;
-  uint64_t *tfull = empty + TC_STAGES;  // [2]
-  uint64_t *tempty = tfull + 2;         // [2]
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
-  __shared__ int s_fail;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rank = (int)cluster_ctarank();
-  const int cid = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
-  const int tiles_n = (a.N + TC_BN - 1) / TC_BN, tiles_m = (a.M + TC_BM - 1) / TC_BM;
-  const int pairs_m = (tiles_m + 1) / 2;
-  const int pairs = pairs_m * tiles_n;
-  const int nk = a.Kp / TC_BK;
-  constexpr uint16_t kBoth = 3;
-  constexpr int kHalfB = TC_B_BYTES / 2;
-
-  if (threadIdx.x == 0) {
-    s_fail = 0;
-    for (int s = 0; s < TC_STAGES; ++s) {
-      mbar_init(full + s, 1);
-      mbar_init(empty + s, 2);  // both CTAs' MMA commits
-    }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(tfull + b, 1);
-      mbar_init(tempty + b, 4);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(2u * TC_BN)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  __syncwarp();
-  cluster_sync_all();  // the peer's barriers exist before any multicast reaches them
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-
-  if (warp == 0) {
-    if (lane == 0) {
-      int g = 0;
-      for (int t = cid; t < pairs && !s_fail; t += nclusters) {
-        int m0p, n0;
-        tile_origin(t, pairs_m, tiles_n, &m0p, &n0);
-        const int m0 = (2 * (m0p / TC_BM) + rank) * TC_BM;
-        for (int kb = 0; kb < nk; ++kb, ++g) {
-          const int s = g % TC_STAGES, r = g / TC_STAGES;
-          if (g >= TC_STAGES && !mbar_wait(empty + s, (uint32_t)((r - 1) & 1), a.err)) {
-            s_fail = 1;
-            break;
-          }
-          mbar_expect_tx(full + s, TC_A_BYTES + TC_B_BYTES);
-          tma_load_2d(sA + s * TC_A_BYTES, &tmA, kb * TC_BK, m0, full + s);
-          tma_load_2d_mc(sB + s * TC_B_BYTES + rank * kHalfB, &tmBh, kb * TC_BK, n0 + rank * (TC_BN / 2), full + s,
-                         kBoth);
-        }
-      }
-      // Before leaving: the last copies into this CTA have landed and both
-      // CTAs' MMAs have released the last slots (their commits reach this
-      // CTA's barriers).
-      for (int q = g - TC_STAGES < 0 ? 0 : g - TC_STAGES; q < g; ++q) {
-        const uint32_t ph = (uint32_t)((q / TC_STAGES) & 1);
-        if (!mbar_try_wait(full + q % TC_STAGES, ph)) mbar_wait(full + q % TC_STAGES, ph, a.err);
-        if (!mbar_try_wait(empty + q % TC_STAGES, ph)) mbar_wait(empty + q % TC_STAGES, ph, a.err);
-      }
-    }
-  } else if (warp == 1) {
-    if (lane == 0) {
-      int g = 0, i = 0;
-      for (int t = cid; t < pairs && !s_fail; t += nclusters, ++i) {
-        const int b = i & 1, u = i >> 1;
-        if (u >= 1 && !mbar_wait(tempty + b, (uint32_t)((u - 1) & 1), a.err)) {
-          s_fail = 1;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
-        for (int kb = 0; kb < nk; ++kb, ++g) {
-          const int s = g % TC_STAGES, r = g / TC_STAGES;
-          if (!mbar_wait(full + s, (uint32_t)(r & 1), a.err)) {
-            s_fail = 1;
-            break;
-          }
-          tc_fence_after();
-          const uint64_t ad = sdesc_k_sw128(smem_u32(sA + s * TC_A_BYTES));
-          const uint64_t bd = sdesc_k_sw128(smem_u32(sB + s * TC_B_BYTES));
-#pragma unroll
-          for (int k = 0; k < TC_BK / 32; ++k) mma_f8(acc, ad + 2 * k, bd + 2 * k, TC_IDESC, (kb | k) != 0 ? 1u : 0u);
-          mma_commit_mc(empty + s, kBoth);
-        }
-        mma_commit(tfull + b);
-        if (s_fail) break;
-      }
-    }
-  } else {
-    const int q4 = warp & 3;
-    int i = 0;
-    for (int t = cid; t < pairs; t += nclusters, ++i) {
-      const int b = i & 1, u = i >> 1;
-      int go = 0;
-      if (lane == 0) go = mbar_wait(tfull + b, (uint32_t)(u & 1), a.err) && !s_fail;
-      go = __shfl_sync(0xffffffffu, go, 0);
-      tc_fence_after();
-      if (!go) break;
-      int m0p, n0;
-      tile_origin(t, pairs_m, tiles_n, &m0p, &n0);
-      const int m0 = (2 * (m0p / TC_BM) + rank) * TC_BM;
-      epilogue_tile(a, tmem, b, q4, lane, m0, n0);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty + b)) : "memory");
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  __syncwarp();
-  cluster_sync_all();  // no remote write or arrive can target this CTA any more
-  if (warp == 1) {
-    __syncwarp();
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * TC_BN) : "memory");
-  }
-}
-
 // Word-major bits -> K-major e4m3 bytes, plus row popcounts.
 // out[r][32 kw + b] = bit b of G[kw][r] ? 1.0 (0x38) : 0.0, columns Kw*32 ..
 // Kp zero; pop[r] += popc of the row's words (pop zeroed by the caller).  A
@@ -653,7 +482,7 @@ gbs_status make_map(CUtensorMap *map, void *base, int rows, int Kp, int box_rows
 static __device__ int g_bmm_tc_err;
 
 // launch forms of bmm_tc_run
-constexpr int kTcPerTile = 0, kTcPersistent = 1, kTcPair = 2;
+constexpr int kTcPerTile = 0, kTcPersistent = 1;
 
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
                       int ldc, cudaStream_t s, int form) {
@@ -673,15 +502,13 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   GBS_TRY(check_launch("bmm tc prologue"));
   CUtensorMap ma, mb;
   GBS_TRY(make_map(&ma, A8.p, M, Kp, TC_BM));
-  GBS_TRY(make_map(&mb, B8.p, N, Kp, form == kTcPair ? TC_BN / 2 : TC_BN));
+  GBS_TRY(make_map(&mb, B8.p, N, Kp, TC_BN));
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
     attr_err = cudaFuncSetAttribute(k_bmm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (attr_err == cudaSuccess)
       attr_err = cudaFuncSetAttribute(k_bmm_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    if (attr_err == cudaSuccess)
-      attr_err = cudaFuncSetAttribute(k_bmm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   });
   if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(k_bmm_tc)");
   int *err = nullptr;
@@ -690,28 +517,7 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   const int tiles = ((N + TC_BN - 1) / TC_BN) * ((M + TC_BM - 1) / TC_BM);
   DeviceInfo di;
   GBS_TRY(device_info(&di));
-  if (form == kTcPair) {
-    // clusters of 2 CTAs, as many as can be resident at once
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(192);
-    cfg.dynamicSmemBytes = TC_SMEM;
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cfg.gridDim = dim3(2 * (unsigned)di.sm_count);
-    int max_clusters = 0;
-    GBS_CUDA_TRY(cudaOccupancyMaxActiveClusters(&max_clusters, (const void *)k_bmm_tc_pair, &cfg));
-    if (max_clusters < 1) return fail(GBS_ERR_UNSUPPORTED, "bmm tc: no CTA pair fits on this device");
-    const int pairs = ((N + TC_BN - 1) / TC_BN) * (((M + TC_BM - 1) / TC_BM + 1) / 2);
-    const int clusters = pairs < max_clusters ? pairs : max_clusters;
-    cfg.gridDim = dim3(2 * (unsigned)clusters);
-    GBS_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_bmm_tc_pair, ma, mb, args));
-  } else if (form == kTcPersistent) {
+  if (form == kTcPersistent) {
     const int grid = tiles < di.sm_count ? tiles : di.sm_count;
     k_bmm_tc_persist<<<grid, 192, TC_SMEM, s>>>(ma, mb, args);
   } else {

@@ -12,94 +12,21 @@
 #include "feat.cuh"
 #include "merge.cuh"
 #include "merge_kernel.cuh"
+#include "spmm_variants.cuh"
 #include "util.cuh"
 
 namespace gbs {
 
-// MINB: CTAs per SM the register budget must allow.  The gathers are
-// latency-bound, and on GB300 more resident warps beat deeper per-warp
-// unrolling: for the 232,965-node / 114.8M-edge graph at F = 256, 32 warps
-// per SM with 2 (FP32) / 4 (BF16) nonzeros in flight per warp measured
-// 7.12 / 5.47 ms against 7.98 / 5.67 ms for 24 warps with 4 / 8 in flight.
-template <int DT, int VEC, int LPR, int CH, int U, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_csr_spmm_merge(MergeArgs a) {
-  MergeKernel<DT, VEC, LPR, CH, U>::run(a);
+gbs_status spmm_select(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out, bool scaled) {
+  if (scaled) return spmm_select_scaled(dt, Fw, vec16, halfwarp, out);
+  return select_variant<false>(dt, Fw, vec16, halfwarp, out);
 }
 
-// ---------------------------------------------------------------------------
-// host side: variant selection, column blocking, grid sizing, workspace
-// ---------------------------------------------------------------------------
 namespace {
-
-constexpr int kThreads = 256;
+constexpr int kThreads = kSpmmThreads;
 constexpr long long kMinEventsPerWarp = 256;
-
-template <int DT, int VEC, int LPR, int CH>
-SpmmVariant mk() {
-  constexpr int UCAP = CH == 1 ? 4 : (CH == 2 ? 2 : 1);
-  constexpr int U = UCAP < LPR ? UCAP : LPR;
-  // register estimate: accumulators (+ blocked partials, FP32 only) + loads
-  // in flight.  Without the partials the half-warp BF16 variant fits 4 CTAs
-  // per SM: 4.21 against 4.78 ms (114.8M-edge graph, F = 256, 2 parts).
-  constexpr int EST = 24 + (DT == DT_F32 ? 2 : 1) * CH * VEC + U * CH * 4 + U;
-  constexpr int MINB = EST <= 64 ? 4 : (EST <= 80 ? 3 : (EST <= 128 ? 2 : 1));
-  return SpmmVariant{(const void *)&k_csr_spmm_merge<DT, VEC, LPR, CH, U, MINB>, VEC, LPR, CH};
-}
-
-// Lanes per row (LPR) and 16-byte chunks per lane (CH) for rows of nvec
-// chunks.  With `halfwarp` (the gathered rows of B fit in half of L2), rows
-// of 17-32 chunks of 16-bit features and 33-64 chunks of FP32 (F = 136..256)
-// run on half-warps, two nonzeros per warp at a time: one shuffle pair then
-// feeds two gathers, which measured 4.8 against 5.3 ms (BF16, 2 parts) and
-// 6.4 against 6.7 ms (FP32, 4 parts) on the 114.8M-edge graph at F = 256.
-// The half-warp variants need more registers (3 instead of 4 CTAs per SM),
-// which costs more than it saves when many gathers go to DRAM.
-template <int DT, int VEC>
-bool pick_lpr_ch(int nvec, bool halfwarp, SpmmVariant *v) {
-  if (nvec <= 1) { *v = mk<DT, VEC, 1, 1>(); return true; }
-  if (nvec <= 2) { *v = mk<DT, VEC, 2, 1>(); return true; }
-  if (nvec <= 4) { *v = mk<DT, VEC, 4, 1>(); return true; }
-  if (nvec <= 8) { *v = mk<DT, VEC, 8, 1>(); return true; }
-  if (nvec <= 16) { *v = mk<DT, VEC, 16, 1>(); return true; }
-  if constexpr (VEC == 8) {
-    if (halfwarp && nvec <= 32) { *v = mk<DT, VEC, 16, 2>(); return true; }
-  }
-  if (nvec <= 32) { *v = mk<DT, VEC, 32, 1>(); return true; }
-  if constexpr (VEC == 4) {
-    if (halfwarp && nvec <= 64) { *v = mk<DT, VEC, 16, 4>(); return true; }
-  }
-  if (nvec <= 64) { *v = mk<DT, VEC, 32, 2>(); return true; }
-  if (nvec <= 128) { *v = mk<DT, VEC, 32, 4>(); return true; }
-  if (nvec <= 256) { *v = mk<DT, VEC, 32, 8>(); return true; }
-  if constexpr (VEC == 1) {
-    if (nvec <= 512) { *v = mk<DT, VEC, 32, 16>(); return true; }
-    if (nvec <= 1024) { *v = mk<DT, VEC, 32, 32>(); return true; }
-  }
-  return false;
-}
-
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
-
 }  // namespace
-
-// Variant for a column block of width Fw.  vec16 = 16-byte vector loads are
-// allowed (aligned pointers, F a multiple of the vector width).
-gbs_status spmm_select(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out) {
-  bool ok = false;
-  if (dt == DT_F32) {
-    if (vec16 && Fw % 4 == 0) ok = pick_lpr_ch<DT_F32, 4>(Fw / 4, halfwarp, out);
-    else ok = pick_lpr_ch<DT_F32, 1>(Fw, halfwarp, out);
-    if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: FP32 features need F <= 1024");
-  } else {
-    if (!vec16 || Fw % 8 != 0)
-      return fail(GBS_ERR_UNSUPPORTED,
-                  "csr spmm: 16-bit features need F % 8 == 0 and 16-byte aligned B/C");
-    ok = dt == DT_BF16 ? pick_lpr_ch<DT_BF16, 8>(Fw / 8, halfwarp, out)
-                       : pick_lpr_ch<DT_F16, 8>(Fw / 8, halfwarp, out);
-    if (!ok) return fail(GBS_ERR_UNSUPPORTED, "csr spmm: 16-bit features need F <= 2048");
-  }
-  return GBS_OK;
-}
 
 // Number of warps (P): one resident wave of the variant, but no warp with
 // fewer than kMinEventsPerWarp merge events.
@@ -166,7 +93,7 @@ gbs_status spmm_col_block(int dt, int ncols, int nnz, int F, bool vec16, int col
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
                        float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base,
-                       int accumulate) {
+                       int accumulate, const float *rowscale, const float *colscale) {
   // the kernels address a row of B by a 32-bit byte pitch
   GBS_REQUIRE(ldb >= 0 && ldb * 4 < (1LL << 32), "csr spmm: row stride of B too large");
   MergeArgs a;
@@ -184,6 +111,8 @@ gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const in
   a.rowptr = rowptr;
   a.colind = colind;
   a.vals = vals;
+  a.rowscale = rowscale;
+  a.colscale = vals ? nullptr : colscale;
   a.B = B;
   a.C = C;
   a.ldp = (int)align_up((size_t)Fw, 4);
@@ -214,14 +143,14 @@ gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, con
 }
 
 gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B, const float *C,
-                     int col_block, SpmmPlan *p, int gathered_rows) {
+                     int col_block, SpmmPlan *p, int gathered_rows, bool scaled) {
   const int vec = dt == DT_F32 ? 4 : 8;
   p->vec16 = aligned16(B) && aligned16(C) && F % vec == 0;
   GBS_TRY(spmm_col_block(dt, ncols, nnz, F, p->vec16, col_block, &p->Fw));
   DeviceInfo di;
   GBS_TRY(device_info(&di));
   const double slice = (double)(gathered_rows >= 0 ? gathered_rows : ncols) * p->Fw * (dt == DT_F32 ? 4 : 2);
-  GBS_TRY(spmm_select(dt, p->Fw, p->vec16, slice <= 0.5 * (double)di.l2_bytes, &p->v));
+  GBS_TRY(spmm_select(dt, p->Fw, p->vec16, slice <= 0.5 * (double)di.l2_bytes, &p->v, scaled));
   GBS_TRY(spmm_warps(p->v, nrows, nnz, &p->P));
   p->nblk = F / p->Fw;
   p->esize = dt == DT_F32 ? 4 : 2;
@@ -237,9 +166,12 @@ gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes
     if (dt != DT_F32 && !vec16) continue;
     for (int Fw = 1; Fw <= F; ++Fw) {
       if (F % Fw != 0) continue;
-      for (int hw = 0; hw < 2; ++hw) {
+      for (int hw = 0; hw < 4; ++hw) {  // bit 0: half-warp rows, bit 1: scaled kernels
         SpmmVariant v;
-        if (spmm_select(dt, Fw, vec16 != 0, hw != 0, &v) != GBS_OK) { clear_error(); continue; }
+        if (spmm_select(dt, Fw, vec16 != 0, (hw & 1) != 0, &v, (hw & 2) != 0) != GBS_OK) {
+          clear_error();
+          continue;
+        }
         int P = 1;
         GBS_TRY(spmm_warps(v, nrows, nnz, &P));
         size_t b = spmm_workspace_bytes(P, Fw);
@@ -256,11 +188,12 @@ gbs_status spmm_workspace_upper(int dt, int nrows, int nnz, int F, size_t *bytes
 
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream, int rp_base, int accumulate) {
+                    cudaStream_t stream, int rp_base, int accumulate, const float *rowscale,
+                    const float *colscale) {
   for (int b = 0; b < p.nblk; ++b) {
     const char *Bb = reinterpret_cast<const char *>(B) + (size_t)b * p.Fw * p.esize;
     GBS_TRY(spmm_launch(p.v, p.P, nrows, nnz, rowptr, colind, vals, Bb, F, p.Fw,
-                        C + (size_t)b * p.Fw, F, ws, stream, rp_base, accumulate));
+                        C + (size_t)b * p.Fw, F, ws, stream, rp_base, accumulate, rowscale, colscale));
   }
   return GBS_OK;
 }

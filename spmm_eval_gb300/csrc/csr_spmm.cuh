@@ -25,7 +25,9 @@ struct SpmmPlan {
 
 // halfwarp: the gathered rows of B fit in half of L2 (enables the half-warp
 // variants for F = 136..256).
-gbs_status spmm_select(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out);
+// scaled: the degree-normalised kernels (rowscale / colscale, binary A).
+gbs_status spmm_select(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out, bool scaled = false);
+gbs_status spmm_select_scaled(int dt, int Fw, bool vec16, bool halfwarp, SpmmVariant *out);
 gbs_status spmm_warps(const SpmmVariant &v, int nrows, int nnz, int *P_out);
 size_t spmm_counter_bytes();
 size_t spmm_workspace_bytes(int P, int Fw);
@@ -38,14 +40,17 @@ gbs_status spmm_check_args(int nrows, int ncols, int nnz, const int *rowptr, con
 // gathered_rows: rows of B the launch actually reads (a column part of the
 // planned form reads ~ncols / K of them; -1 = ncols).
 gbs_status spmm_plan(int dt, int nrows, int ncols, int nnz, int F, const void *B, const float *C,
-                     int col_block, SpmmPlan *p, int gathered_rows = -1);
+                     int col_block, SpmmPlan *p, int gathered_rows = -1, bool scaled = false);
+// rowscale / colscale (optional, vals null): the degree-normalised product
+// C[r] = rowscale[r] * sum_c colscale[c] B[c] over the stored entries of row r.
 gbs_status spmm_launch(const SpmmVariant &v, int P, int nrows, int nnz, const int *rowptr,
                        const int *colind, const float *vals, const void *B, long long ldb, int Fw,
                        float *C, long long ldc, void *ws, cudaStream_t stream, int rp_base = 0,
-                       int accumulate = 0);
+                       int accumulate = 0, const float *rowscale = nullptr, const float *colscale = nullptr);
 gbs_status spmm_run(const SpmmPlan &p, int nrows, int nnz, const int *rowptr, const int *colind,
                     const float *vals, const void *B, int F, float *C, void *ws,
-                    cudaStream_t stream, int rp_base = 0, int accumulate = 0);
+                    cudaStream_t stream, int rp_base = 0, int accumulate = 0,
+                    const float *rowscale = nullptr, const float *colscale = nullptr);
 
 // Column partition of a CSR matrix (csr_spmm_plan.cu): part p holds, for
 // every row, the entries whose column lies in [p S, (p + 1) S), S =

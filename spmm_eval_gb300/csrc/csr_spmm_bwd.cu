@@ -94,6 +94,8 @@ gbs_status bwd_launch(const SpmmVariant &v, int n, int nnz, const int *rowptr, c
   a.rp_base = 0;
   a.colind = colind;
   a.vals = vals;
+  a.rowscale = nullptr;
+  a.colscale = nullptr;
   a.B = dC;
   a.C = dB;
   a.ldp = (int)align_up((size_t)F, 4);

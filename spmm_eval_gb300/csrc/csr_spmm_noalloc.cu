@@ -16,40 +16,36 @@
 // calls share it, so two calls that can overlap on the GPU (different
 // streams, or different host threads on one device) race on it and must be
 // serialised by the caller.
-#include <mutex>
-
 #include "common.cuh"
 #include "csr_spmm.cuh"
 
 namespace gbs {
 
-// 8 MiB: enough for the partial sums of one full resident wave of warps on
-// a 152-SM GPU up to F = 1024 FP32 columns per launch; the warp count is
-// reduced when a shape would need more.
+// 8 MiB.  The scratch of a launch is a fixed counter region (one int per
+// warp the device can hold) plus two partial-sum rows of F floats per warp,
+// so 8 MiB holds a full resident wave of warps up to about F = 128 FP32
+// columns; wider rows run with fewer warps (fit_warps), which is correct but
+// slower, down to 8 KiB per warp at F = 1024.  Widths the library does not
+// support at all fail as they do in gbs_csr_spmm (GBS_ERR_UNSUPPORTED).
 constexpr size_t kNoAllocScratchBytes = 8u << 20;
 
 static __device__ __align__(256) unsigned char g_spmm_scratch[kNoAllocScratchBytes];
 
 namespace {
 
-// Device address of g_spmm_scratch, looked up once per device.  In host code
-// the name g_spmm_scratch is only a host-side stand-in for the symbol; the
+// Device address of g_spmm_scratch on the current device.  In host code the
+// name g_spmm_scratch is only a host-side stand-in for the symbol; the
 // address a kernel may use comes from cudaGetSymbolAddress with that device
-// current.
+// current.  It is looked up on every call (no allocation, cheap) rather than
+// cached, so a call after cudaDeviceReset or with a new primary context never
+// uses an address from the old context.  The first lookup in a context loads
+// the library's device code (which reserves the array), so that first call
+// must come before any stream capture.
 gbs_status scratch_address(void **out) {
-  static std::mutex mu;
-  static void *addr[64] = {nullptr};
-  int dev = 0;
-  GBS_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "csr spmm noalloc: device ordinal >= 64");
-  std::lock_guard<std::mutex> lock(mu);
-  if (addr[dev] == nullptr) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_spmm_scratch)");
-    addr[dev] = p;
-  }
-  *out = addr[dev];
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_spmm_scratch)");
+  *out = p;
   return GBS_OK;
 }
 
@@ -78,6 +74,8 @@ extern "C" gbs_status gbs_csr_spmm_noalloc(int nrows, int ncols, int nnz, const 
   GBS_TRY(spmm_plan(dt, nrows, ncols, nnz, F, B, C, 0, &p));
   p.P = fit_warps(p.P, p.Fw);
   p.ws_bytes = spmm_workspace_bytes(p.P, p.Fw);
+  // a guard: with one warp every supported width fits (at most 16 KiB of
+  // partial rows beside the counters)
   if (p.ws_bytes > kNoAllocScratchBytes)
     return fail(GBS_ERR_INVALID_ARG,
                 "csr spmm noalloc: F = " + std::to_string(F) + " needs " +

@@ -24,6 +24,10 @@ struct gbs_csr_spmm_plan {
   int nrows, ncols, nnz, F;
   gbs_dtype btype;
   gbs::ColumnParts parts;
+  // degree-normalised binary A: copies of the row and column scales (null
+  // for a plan with stored values)
+  float *rowscale = nullptr, *colscale = nullptr;
+  bool scaled = false;
 };
 
 namespace gbs {
@@ -214,10 +218,38 @@ gbs_status partition_columns(int nrows, int ncols, int nnz, const int *rowptr, c
 
 using namespace gbs;
 
+static gbs_status plan_create(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                              const float *vals, const float *rowscale, const float *colscale,
+                              gbs_dtype btype, int F, int parts, gbs_stream_t stream,
+                              gbs_csr_spmm_plan **out);
+
+static void plan_free(gbs_csr_spmm_plan *P) {
+  if (!P) return;
+  P->parts.release();
+  if (P->rowscale) cudaFree(P->rowscale);
+  if (P->colscale) cudaFree(P->colscale);
+  delete P;
+}
+
 extern "C" gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
                                                const float *vals, gbs_dtype btype, int F, int parts,
                                                gbs_stream_t stream, gbs_csr_spmm_plan **out) {
   clear_error();
+  return plan_create(nrows, ncols, nnz, rowptr, colind, vals, nullptr, nullptr, btype, F, parts, stream, out);
+}
+
+extern "C" gbs_status gbs_csr_spmm_plan_create_scaled(int nrows, int ncols, int nnz, const int *rowptr,
+                                                      const int *colind, const float *rowscale,
+                                                      const float *colscale, gbs_dtype btype, int F,
+                                                      int parts, gbs_stream_t stream, gbs_csr_spmm_plan **out) {
+  clear_error();
+  return plan_create(nrows, ncols, nnz, rowptr, colind, nullptr, rowscale, colscale, btype, F, parts, stream, out);
+}
+
+static gbs_status plan_create(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                              const float *vals, const float *rowscale, const float *colscale,
+                              gbs_dtype btype, int F, int parts, gbs_stream_t stream,
+                              gbs_csr_spmm_plan **out) {
   GBS_REQUIRE(out != nullptr, "spmm plan: null output");
   *out = nullptr;
   GBS_REQUIRE(btype == GBS_F32 || btype == GBS_BF16 || btype == GBS_F16, "spmm plan: bad dtype");
@@ -231,10 +263,25 @@ extern "C" gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz, co
   P->nnz = nnz;
   P->F = F;
   P->btype = btype;
+  P->scaled = rowscale != nullptr || colscale != nullptr;
   gbs_status st = partition_columns(nrows, ncols, nnz, rowptr, colind, vals, nullptr, K, (cudaStream_t)stream,
                                     &P->parts);
+  // the scales are copied, so the caller's arrays need not outlive the plan
+  auto copy_scale = [&](const float *src, int count, float **dst) -> gbs_status {
+    if (!src || count == 0) return GBS_OK;
+    GBS_CUDA_TRY(cudaMalloc(dst, sizeof(float) * (size_t)count));
+    GBS_CUDA_TRY(cudaMemcpyAsync(*dst, src, sizeof(float) * (size_t)count, cudaMemcpyDeviceToDevice,
+                                 (cudaStream_t)stream));
+    return GBS_OK;
+  };
+  if (st == GBS_OK) st = copy_scale(rowscale, nrows, &P->rowscale);
+  if (st == GBS_OK) st = copy_scale(colscale, ncols, &P->colscale);
+  if (st == GBS_OK && (P->rowscale || P->colscale)) {
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "spmm plan: scale copies");
+  }
   if (st != GBS_OK) {
-    delete P;
+    plan_free(P);
     return st;
   }
   *out = P;
@@ -250,10 +297,7 @@ extern "C" gbs_status gbs_csr_spmm_plan_parts(const gbs_csr_spmm_plan *P, int *p
 
 extern "C" gbs_status gbs_csr_spmm_plan_destroy(gbs_csr_spmm_plan *P) {
   clear_error();
-  if (P) {
-    P->parts.release();
-    delete P;
-  }
+  plan_free(P);
   return GBS_OK;
 }
 
@@ -267,10 +311,11 @@ extern "C" gbs_status gbs_csr_spmm_planned(const gbs_csr_spmm_plan *P, const voi
   const ColumnParts &cp = P->parts;
   for (int p = 0; p < cp.K; ++p) {
     SpmmPlan sp;
-    GBS_TRY(spmm_plan(dt, P->nrows, P->ncols, cp.nnz[p], P->F, B, C, 0, &sp, (P->ncols + cp.K - 1) / cp.K));
+    GBS_TRY(spmm_plan(dt, P->nrows, P->ncols, cp.nnz[p], P->F, B, C, 0, &sp, (P->ncols + cp.K - 1) / cp.K,
+                      P->scaled));
     GBS_REQUIRE(ws != nullptr && ws_bytes >= sp.ws_bytes, "spmm planned: workspace missing or too small");
     GBS_TRY(spmm_run(sp, P->nrows, cp.nnz[p], cp.rowptr[p], cp.colind[p], cp.vals[p], B, P->F, C, ws,
-                     (cudaStream_t)stream, 0, p > 0 ? 1 : 0));
+                     (cudaStream_t)stream, 0, p > 0 ? 1 : 0, P->rowscale, P->colscale));
   }
   return GBS_OK;
 }

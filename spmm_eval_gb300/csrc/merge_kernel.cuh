@@ -37,6 +37,11 @@ struct MergeArgs {
   int rp_base;
   const int *colind;
   const float *vals;  // may be null: binary A
+  // degree-normalised binary A (vals null): entry (r, c) counts as
+  // colscale[c] and row r of the result is multiplied by rowscale[r]; either
+  // may be null (= 1).  Forward kernels only.
+  const float *rowscale;
+  const float *colscale;
   const void *B;
   float *C;
   float *partials;  // [2P][ldp]
@@ -51,7 +56,9 @@ struct MergeArgs {
   const int *perm;   // entry e of this matrix -> index in dvals
 };
 
-template <int DT, int VEC, int LPR, int CH, int U, bool SD = false>
+// SC: degree-normalised binary A (rowscale / colscale, forward only);
+// a separate instantiation, so the other kernels carry no extra registers.
+template <int DT, int VEC, int LPR, int CH, int U, bool SD = false, bool SC = false>
 struct MergeKernel {
   static constexpr int NSUB = 32 / LPR;
   static constexpr int KPS = LPR;  // nonzeros per sub-group in a batch of 32
@@ -95,6 +102,26 @@ struct MergeKernel {
       for (int c = 0; c < CH; ++c) F_::fma(bs[c], vv[u], bv[u][c]);
   }
 
+  // Value of entry e (column col): the stored value (or 1: binary A), or
+  // the column's scale of a degree-normalised binary A.
+  static __device__ __forceinline__ float entry_value(const MergeArgs &a, int e, int col) {
+    if constexpr (SC) {
+      return a.colscale ? __ldg(a.colscale + col) : 1.f;
+    } else {
+      return a.vals ? ld_stream_f32(a.vals + e) : 1.f;
+    }
+  }
+
+  static __device__ __forceinline__ void scale_row(const MergeArgs &a, int r, float (&acc)[CH][VEC]) {
+    if constexpr (!SC) return;
+    if (!a.rowscale) return;
+    const float s = __ldg(a.rowscale + r);
+#pragma unroll
+    for (int c = 0; c < CH; ++c)
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) acc[c][q] *= s;
+  }
+
   // Sum nonzeros [jb, je) of one row into acc (this lane's columns, this
   // lane's sub-group share).
   static __device__ __forceinline__ void accumulate(const MergeArgs &a, int jb, int je,
@@ -126,7 +153,7 @@ struct MergeKernel {
     float nx_val = 0.f;
     if (jb + lane < je) {
       nx_col = ld_stream_i32(a.colind + jb + lane);
-      nx_val = a.vals ? ld_stream_f32(a.vals + jb + lane) : 1.f;
+      nx_val = entry_value(a, jb + lane, nx_col);
     }
     for (int base = jb; base < je; base += 32) {
       const int n_valid = min(32, je - base);
@@ -135,7 +162,7 @@ struct MergeKernel {
       // the next batch of this row is loaded while this one is gathered
       if (base + 32 + lane < je) {
         nx_col = ld_stream_i32(a.colind + base + 32 + lane);
-        nx_val = a.vals ? ld_stream_f32(a.vals + base + 32 + lane) : 1.f;
+        nx_val = entry_value(a, base + 32 + lane, nx_col);
       }
       // blocked summation: each batch of 32 nonzeros is summed into a fresh
       // partial that is then added to the row total (error ~ sqrt(32) +
@@ -328,6 +355,11 @@ struct MergeKernel {
         load_vec_cg<VEC>(a.partials + (size_t)(2 * w2) * a.ldp + (size_t)chunk * VEC, x);
 #pragma unroll
         for (int q = 0; q < VEC; ++q) sum[q] += x[q];
+        if (SC && a.rowscale) {
+          const float s = __ldg(a.rowscale + r);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) sum[q] *= s;
+        }
         float *dst = a.C + (size_t)r * a.ldc + (size_t)chunk * VEC;
         if (a.accumulate) {
           load_vec_cg<VEC>(dst, x);
@@ -360,6 +392,7 @@ struct MergeKernel {
       if constexpr (SD) load_h(a, r, lane, h);
       accumulate(a, j, re, lane, acc, h);
       if (j == rb) {
+        scale_row(a, r, acc);
         if (a.accumulate) add_row(a, a.C + (size_t)r * a.ldc, lane, acc);
         else write_row<true>(a, a.C + (size_t)r * a.ldc, lane, acc);
       } else {  // head piece: the row started in an earlier warp

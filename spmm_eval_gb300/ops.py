@@ -313,7 +313,7 @@ def b2sr_aligned(Ab: B2SR):
 # Dense binary matmul (word-major operands, ToBit32ColUd layout)
 # ---------------------------------------------------------------------------
 BMM_XOR, BMM_AND, BMM_SIGNED = 0, 1, 2
-BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA, BMM_ALGO_TC, BMM_ALGO_TC_PERSIST, BMM_ALGO_TC_PAIR = 0, 1, 2, 3, 4, 5
+BMM_ALGO_DEFAULT, BMM_ALGO_POPC, BMM_ALGO_MMA, BMM_ALGO_TC, BMM_ALGO_TC_PERSIST = 0, 1, 2, 3, 4
 
 
 def bmm_tc_timeouts() -> int:

@@ -57,15 +57,22 @@ def test_empty_matrix_is_a_no_op(built_lib):
     _lib.call("gbs_csr_spmm", 0, 0, 0, None, None, None, None, _lib.GBS_F32, 8, None, None, 0, None)
 
 
-def test_bench_reads_committed_measurements():
-    """bench.py's roofline inputs come from the committed ncu / probe
-    summaries: DRAM bytes per step and the L2 -> SM gather ceiling."""
+def test_bench_roofline_inputs():
+    """bench.py's HBM roofline takes the step's DRAM bytes from the committed
+    ncu summary; the L2 -> SM gather ceiling is measured by the probe in the
+    run itself, so without a GPU it is absent rather than read from a file.
+    The plain relative error skips entries below the stated floor."""
     import importlib.util
+
+    import torch
     spec = importlib.util.spec_from_file_location("bench_mod", HEADER.parent.parent / "bench.py")
     bench = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bench)
     traffic = bench.profile_traffic()
     assert traffic is not None and 1e9 < traffic < 1e11
-    ceil = bench.gather_ceiling()
-    assert ceil is not None and set(ceil) == {"f32", "bf16"}
-    assert all(10.0 < v < 40.0 for v in ceil.values())
+    if not torch.cuda.is_available():
+        assert bench.gather_ceiling() is None
+    ref = torch.tensor([[10.0, -10.0, 1e-9, 0.0]], dtype=torch.float64)
+    got = torch.tensor([[10.1, -10.0, 5.0, 1.0]])
+    p = bench.plain_rel_err(got, ref)
+    assert p["entries"] == 2 and abs(p["max"] - 0.01) < 1e-6

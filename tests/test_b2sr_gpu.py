@@ -279,9 +279,17 @@ def test_fbf_equals_cusparse_on_pm1(cuda, cusparse_ref, F):
 
 
 @pytest.mark.parametrize("ts", TILES)
-@pytest.mark.parametrize("F", [1, 32, 64, 96, 256, 1024])
+@pytest.mark.parametrize("F", [1, 32, 64, 96, 256, 512, 1024])
 def test_bmm_bit_exact(cuda, ts, F):
-    name, n, m, rp, ci = GRAPHS[4] if F <= 256 else GRAPHS[2]
+    """Every width on the flickr-shaped graph, whose hub block-rows go to the
+    hub pass (k_b2sr_bmm_hubs, up to 32 words per row at F = 1024), and on a
+    small random graph."""
+    for gi in (4, 2):
+        _bmm_case(cuda, ts, F, gi)
+
+
+def _bmm_case(cuda, ts, F, gi):
+    name, n, m, rp, ci = GRAPHS[gi]
     brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
     X = G.normal(F + ts, 8, (m, F))
     Xw = ops.pack_sign_rows(X.to(cuda))

@@ -165,6 +165,34 @@ def test_reddit_scale_properties(cuda):
     assert mx <= 1e-5, mx
 
 
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16, torch.float32])
+def test_reddit_scale_feature_types(cuda, dtype):
+    """The 232,965-node graph at F = 256 with FP32, BF16 or FP16 features
+    through the planned SpMM, on sampled rows incl. the 16 largest hubs:
+    scaled error <= 1e-5 against the FP64 product of the features as stored
+    (accumulation), <= 1e-2 for 16-bit features against the FP64 product of
+    the FP32 features (incl. the storage rounding), and the plain relative
+    error |C - C64| / |C64| <= 1e-2 (16-bit) / 1e-5 (FP32) over the entries
+    whose |C64| is at least the RMS of C64 on those rows."""
+    g = G.gcn_normalize(G.reddit_like(device=cuda))
+    A = ops.CSR(g.rowptr, g.colind, g.vals, g.nrows, g.ncols)
+    B32 = G.normal(4, 5, (g.ncols, 256), device=cuda)
+    Bx = B32.to(dtype)
+    C = ops.SpmmPlan(A, 256, dtype).run(Bx)
+    deg = (g.rowptr[1:] - g.rowptr[:-1]).cpu()
+    rows = torch.cat([torch.topk(deg, 16).indices, torch.arange(0, g.nrows, 1999)]).numpy()
+    rp, ci, va = g.rowptr.cpu().numpy(), g.colind.cpu().numpy(), g.vals.cpu().numpy()
+    got = C.cpu().numpy()[rows]
+    ref_s, mag_s = oracle.csr_spmm_f64(rp, ci, va, Bx.float().cpu().numpy(), rows=rows)
+    assert oracle.rel_err(got, ref_s, mag_s)[0] <= 1e-5
+    ref, mag = oracle.csr_spmm_f64(rp, ci, va, B32.cpu().numpy(), rows=rows)
+    assert oracle.rel_err(got, ref, mag)[0] <= (1e-2 if dtype != torch.float32 else 1e-5)
+    floor = float(np.sqrt(np.mean(ref ** 2)))
+    keep = np.abs(ref) >= floor
+    plain = float(np.max(np.abs(got[keep] - ref[keep]) / np.abs(ref[keep])))
+    assert plain <= (1e-2 if dtype != torch.float32 else 1e-5), plain
+
+
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("cb", [8, 32, 64, 128, 256])
 def test_column_blocks(cuda, dtype, cb):
