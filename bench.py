@@ -390,9 +390,17 @@ def other_configs(dev, timed, reps):
     ms = mean_ms(timed, lambda: ops.bmm_b1(Aw, Bw, ops.BMM_XOR, out=Co), reps, "bmm8192")
     ms_popc = mean_ms(timed, lambda: ops.bmm_b1(Aw, Bw, ops.BMM_XOR, ops.BMM_ALGO_POPC, out=Co), reps,
                       "bmm8192_popc")
+    del Co
+    words = torch.empty(256 * 8192, dtype=torch.int32, device=dev)
+    ms_bin = mean_ms(timed, lambda: ops.bmm_bin(Aw, Bw, words, 8192, 8192, 8192, False, ops.BIN_FUSED), reps,
+                     "bin8192_fused")
+    ms_bin2 = mean_ms(timed, lambda: ops.bmm_bin(Aw, Bw, words, 8192, 8192, 8192, False, ops.BIN_COUNTS), reps,
+                      "bin8192_counts")
     out["bmm_8192"] = {"ms": round(ms, 4), "pbitops": round(2 * 8192 ** 3 / (ms * 1e-3) / 1e15, 3),
-                       "popc_ms": round(ms_popc, 4), "timeouts": ops.bmm_tc_timeouts()}
-    del Aw, Bw, Co
+                       "popc_ms": round(ms_popc, 4),
+                       "bin_words_fused_ms": round(ms_bin, 4), "bin_words_two_pass_ms": round(ms_bin2, 4),
+                       "timeouts": ops.bmm_tc_timeouts()}
+    del Aw, Bw, words
 
     # GCN layer on the normalised flickr-shaped graph
     gn = G.gcn_normalize(g)
@@ -488,6 +496,18 @@ def run_ours(args):
     ms_bf16 = sum(timed(step_bf16, args.steps, "timed_bf16")) / args.steps
     ms_f16 = sum(timed(step_f16, args.steps, "timed_f16")) / args.steps
 
+    # the same product with the normalisation in the kernel: binary A plus
+    # the D^-1/2 factors (no value stream), FP32 and BF16 features
+    Apat = ops.CSR(g.rowptr, g.colind, None, n, n)
+    dinv = ops.degree_rsqrt(Apat)
+    pn32 = ops.SpmmPlan(Apat, F, torch.float32, rowscale=dinv, colscale=dinv)
+    pn16 = ops.SpmmPlan(Apat, F, torch.bfloat16, rowscale=dinv, colscale=dinv)
+    Cn = torch.empty_like(C)
+    Cnh = torch.empty_like(C)
+    ms_n32 = mean_ms(timed, lambda: pn32.run(B, out=Cn, workspace=ws), args.steps, "timed_norm_f32", warm=3)
+    ms_n16 = mean_ms(timed, lambda: pn16.run(Bh, out=Cnh, workspace=ws), args.steps, "timed_norm_bf16", warm=3)
+    del pn32, pn16
+
     # forward + backward of Y = A H: fwd SpMM, bwd A^T dY (cached transpose)
     # and SDDMM for d(values); FP32 vs BF16 features (H, dY), FP32 accumulate
     T = ops.CSRTranspose(ops.CSR(g.rowptr, g.colind, None, n, n))
@@ -540,11 +560,12 @@ def run_ours(args):
     ref, mag = fp64_rows(g_cpu, B_cpu, rows)
     rd = rows.to(dev)
     errs = {}
-    for tag, Cx in (("f32", C), ("bf16_features", Ch), ("fp16_features", Cf)):
+    for tag, Cx in (("f32", C), ("bf16_features", Ch), ("fp16_features", Cf), ("normalized_f32", Cn),
+                    ("normalized_bf16_features", Cnh)):
         got = Cx[rd].cpu()
         mx, mean = rel_err(got, ref, mag)
         errs[tag] = {"max": mx, "mean": mean, "plain": plain_rel_err(got, ref)}
-    del Ch, Cf, Bh, Bf
+    del Ch, Cf, Bh, Bf, Cn, Cnh
 
     # the other configurations
     others = None
@@ -611,6 +632,11 @@ def run_ours(args):
         "bf16": {"ms_per_step": round(ms_bf16, 4),
                  "gbs_gather_model": round(bytes_bf16 / (ms_bf16 * 1e-3) / 1e9, 1),
                  "speedup_vs_f32": round(ms_f32 / ms_bf16, 3)},
+        "normalized": {"what": "the same SpMM with binary A and the D^-1/2 factors applied in the kernel "
+                                "(gbs_csr_spmm_plan_create_scaled: no value stream), planned",
+                       "f32_ms": round(ms_n32, 4), "bf16_ms": round(ms_n16, 4),
+                       "f32_speedup_vs_valued": round(ms_f32 / ms_n32, 3),
+                       "bf16_speedup_vs_valued": round(ms_bf16 / ms_n16, 3)},
         "fp16": {"ms_per_step": round(ms_f16, 4),
                  "gbs_gather_model": round(bytes_bf16 / (ms_f16 * 1e-3) / 1e9, 1),
                  "speedup_vs_f32": round(ms_f32 / ms_f16, 3)},

@@ -416,12 +416,20 @@ GBS_API gbs_status gbs_bmm32_arow_brow(const uint32_t *d_A, const uint32_t *d_B,
 /* Drop-ins for BMM32_BIN (mm.cu:79-105) and BMM32S_BIN (:108-125): bit =
  * (n - 2*xor >= 0) with n the number of K bits, 32 output columns per word,
  * first column in bit 31, stored at C[by*m + r] (BIN) or
- * C[(r/32)*k*32 + by*32 + r%32] (S_BIN).  m, k multiples of 32.  Allocates
- * an m x k int32 temporary (stream-ordered). */
+ * C[(r/32)*k*32 + by*32 + r%32] (S_BIN).  m, k multiples of 32.  The
+ * persistent tcgen05 GEMM thresholds its counts in the epilogue and writes
+ * only the words (no count matrix); temporaries as gbs_bmm_b1 algo 4. */
 GBS_API gbs_status gbs_bmm32_bin(const uint32_t *d_A, const uint32_t *d_B, uint32_t *d_C,
                          int m, int n, int k, gbs_stream_t stream);
 GBS_API gbs_status gbs_bmm32s_bin(const uint32_t *d_A, const uint32_t *d_B, uint32_t *d_C,
                           int m, int n, int k, gbs_stream_t stream);
+/* The sign-word product of gbs_bmm32_bin (layout 0) / gbs_bmm32s_bin
+ * (layout 1) with the algorithm chosen: algo 0 = thresholded in the tcgen05
+ * epilogue (what the drop-ins run), 1 = int32 XOR counts into an m x k
+ * temporary, then a separate sign-word pass.  Same words either way.  No
+ * counterpart in the reference beyond the two kernels named above. */
+GBS_API gbs_status gbs_bmm_bin(const uint32_t *d_A, const uint32_t *d_B, uint32_t *d_C, int m,
+                       int n, int k, int layout, int algo, gbs_stream_t stream);
 
 /* CSR SpMM that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not allocate while they run (a

@@ -64,6 +64,9 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_spmm_host_ctx_destroy": (st, [p]),
     "gbs_csr_spmm_host": (st, [p, i32, i32, i32, p, p, p, p, i32, i32, p, p]),
     "gbs_csr_spmm_plan_create": (st, [i32, i32, i32, p, p, p, i32, i32, i32, p, C.POINTER(p)]),
+    "gbs_csr_spmm_plan_create_scaled": (st, [i32, i32, i32, p, p, p, p, i32, i32, i32, p, C.POINTER(p)]),
+    "gbs_csr_spmm_scaled": (st, [i32, i32, i32, p, p, p, p, p, i32, i32, p, p, sz, p]),
+    "gbs_degree_rsqrt": (st, [i32, p, p, p]),
     "gbs_csr_spmm_plan_parts": (st, [p, pi32]),
     "gbs_csr_spmm_planned": (st, [p, p, p, p, sz, p]),
     "gbs_csr_spmm_plan_destroy": (st, [p]),
@@ -95,6 +98,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_bmm32_arow_brow": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm32_bin": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm32s_bin": (st, [p, p, p, i32, i32, i32, p]),
+    "gbs_bmm_bin": (st, [p, p, p, i32, i32, i32, i32, i32, p]),
 }
 
 

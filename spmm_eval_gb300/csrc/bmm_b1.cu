@@ -250,7 +250,8 @@ __global__ void k_sign_words(const int32_t *__restrict__ X, int m, int k, int nb
 
 // form: 0 = one CTA per tile, 1 = persistent
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
-                      int ldc, cudaStream_t s, int form);
+                      int ldc, cudaStream_t s, int form, uint32_t *Cbits = nullptr, int bin_layout = 0,
+                      int nbits = 0);
 gbs_status bmm_tc_error_count(int *out);
 
 gbs_status bmm_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int algo,
@@ -326,19 +327,37 @@ extern "C" gbs_status gbs_bmm32_arow_brow(const uint32_t *A, const uint32_t *B, 
                  (cudaStream_t)stream);
 }
 
-static gbs_status bin_common(const uint32_t *A, const uint32_t *B, uint32_t *C, int m, int n, int k,
-                             int layout, cudaStream_t s) {
+// Sign words of the binary GEMM.  algo 0 (default): the persistent tcgen05
+// kernel thresholds the counts in its epilogue and writes only the words;
+// algo 1: the int32 XOR counts of the default GEMM into an m x k temporary,
+// then k_sign_words (kept as the cross-check and the timing baseline).
+static gbs_status bin_run(const uint32_t *A, const uint32_t *B, uint32_t *C, int m, int n, int k,
+                          int layout, int algo, cudaStream_t s) {
   GBS_REQUIRE(m >= 0 && k >= 0 && n >= 1, "bmm32 bin: bad sizes");
   GBS_REQUIRE(m % 32 == 0 && k % 32 == 0, "bmm32 bin: m and k must be multiples of 32 (as the reference's grid)");
+  GBS_REQUIRE(layout == 0 || layout == 1, "bmm bin: layout must be 0 (BMM32_BIN) or 1 (BMM32S_BIN)");
+  GBS_REQUIRE(algo == 0 || algo == 1, "bmm bin: algo must be 0 (fused) or 1 (counts, then sign words)");
   if (m == 0 || k == 0) return GBS_OK;
   GBS_REQUIRE(A && B && C, "bmm32 bin: null pointer");
   const int Kw = (n + 31) / 32;
+  if (algo == 0) return bmm_tc_run(A, B, m, k, Kw, MODE_XOR, nullptr, nullptr, k, s, 1, C, layout, n);
   DevBuf X;
   GBS_TRY(X.alloc(sizeof(int32_t) * (size_t)m * k, s));
   GBS_TRY(bmm_run(A, B, m, k, Kw, MODE_XOR, 0, X.as<int32_t>(), nullptr, k, s));
   const long long warps = (long long)m * (k / 32);
   k_sign_words<<<(int)((warps * 32 + 255) / 256), 256, 0, s>>>(X.as<int32_t>(), m, k, n, layout, C);
   return check_launch("k_sign_words");
+}
+
+static gbs_status bin_common(const uint32_t *A, const uint32_t *B, uint32_t *C, int m, int n, int k,
+                             int layout, cudaStream_t s) {
+  return bin_run(A, B, C, m, n, k, layout, 0, s);
+}
+
+extern "C" gbs_status gbs_bmm_bin(const uint32_t *A, const uint32_t *B, uint32_t *C, int m, int n, int k,
+                                  int layout, int algo, gbs_stream_t stream) {
+  clear_error();
+  return bin_run(A, B, C, m, n, k, layout, algo, (cudaStream_t)stream);
 }
 
 extern "C" gbs_status gbs_bmm32_bin(const uint32_t *A, const uint32_t *B, uint32_t *C, int m, int n, int k,

@@ -51,6 +51,13 @@ struct BmmTcArgs {
   float *Cf;
   int ldc;
   int *err;
+  // sign-word output (instead of C / Cf): bit = (nbits - 2 xor >= 0), 32
+  // columns per word, first column in bit 31; layout 0 = BMM32_BIN
+  // (Cbits[(c / 32) * M + r]), 1 = BMM32S_BIN (Cbits[(r / 32) * N * 32 +
+  // c / 32 * 32 + r % 32]); M, N multiples of 32
+  uint32_t *Cbits;
+  int bin_layout;
+  int nbits;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -131,7 +138,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 // Epilogue of one 128 x 256 tile held in TMEM accumulator b: warp quarter
 // q4 reads its 32 lanes (= rows m0 + 32 q4 + lane) 32 columns at a time and
-// writes the counts (int32 or float C).
+// writes the counts (int32 or float C), or -- with Cbits -- thresholds the
+// 32 XOR counts a lane holds for its row into one sign word (the lane owns
+// the whole word, so no shuffle or ballot) and writes only the words: 1/32
+// of the int32 count matrix, and no second pass over it.
 __device__ __forceinline__ void epilogue_tile(const BmmTcArgs &a, uint32_t tmem, int b, int q4, int lane, int m0,
                                               int n0) {
   const int Kbits = 32 * a.Kw;
@@ -142,6 +152,20 @@ __device__ __forceinline__ void epilogue_tile(const BmmTcArgs &a, uint32_t tmem,
     uint32_t v[32];
     tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * TC_BN + cb * 32), v);
     const int c0 = n0 + cb * 32;
+    if (a.Cbits) {
+      if (row < a.M && c0 < a.N) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int andc = (int)__uint_as_float(v[q]);
+          const int xr = par + __ldg(a.pb + c0 + q) - 2 * andc;
+          word = (word << 1) | (a.nbits - 2 * xr >= 0 ? 1u : 0u);
+        }
+        if (a.bin_layout == 0) a.Cbits[(size_t)(c0 >> 5) * a.M + row] = word;
+        else a.Cbits[(size_t)(row >> 5) * a.N * 32 + (size_t)c0 + (row & 31)] = word;
+      }
+      continue;
+    }
     if (row < a.M) {
 #pragma unroll
       for (int q = 0; q < 32; q += 4) {
@@ -485,8 +509,10 @@ static __device__ int g_bmm_tc_err;
 constexpr int kTcPerTile = 0, kTcPersistent = 1;
 
 gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw, int mode, int32_t *C, float *Cf,
-                      int ldc, cudaStream_t s, int form) {
+                      int ldc, cudaStream_t s, int form, uint32_t *Cbits, int bin_layout, int nbits) {
   GBS_REQUIRE(M % 4 == 0 && N % 4 == 0 && ldc % 4 == 0, "bmm tc: M, N (and ldc) must be multiples of 4");
+  GBS_REQUIRE(!Cbits || (M % 32 == 0 && N % 32 == 0 && mode == 0),
+              "bmm tc: sign words need M, N multiples of 32 and XOR counts");
   GBS_REQUIRE((long long)Kw * 32 < (1ll << 24), "bmm tc: K must be < 2^24 bits (exact FP32 accumulation)");
   const int Kp = (Kw * 32 + TC_BK - 1) / TC_BK * TC_BK;
   DevBuf A8, B8, pa, pb;
@@ -513,7 +539,7 @@ gbs_status bmm_tc_run(const uint32_t *A, const uint32_t *B, int M, int N, int Kw
   if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(k_bmm_tc)");
   int *err = nullptr;
   GBS_CUDA_TRY(cudaGetSymbolAddress((void **)&err, g_bmm_tc_err));
-  BmmTcArgs args{M, N, Kw, Kp, mode, pa.as<int>(), pb.as<int>(), C, Cf, ldc, err};
+  BmmTcArgs args{M, N, Kw, Kp, mode, pa.as<int>(), pb.as<int>(), C, Cf, ldc, err, Cbits, bin_layout, nbits};
   const int tiles = ((N + TC_BN - 1) / TC_BN) * ((M + TC_BM - 1) / TC_BM);
   DeviceInfo di;
   GBS_TRY(device_info(&di));

@@ -112,16 +112,54 @@ def csr_spmm(A: CSR, B: torch.Tensor, out: torch.Tensor | None = None,
     return out
 
 
+def degree_rsqrt(A: CSR) -> torch.Tensor:
+    """D^-1/2 of A's row counts (FP64 on the device, rounded to FP32; 0 for
+    an empty row)."""
+    A.validate_layout()
+    out = torch.empty(A.nrows, dtype=torch.float32, device=A.rowptr.device)
+    _lib.call("gbs_degree_rsqrt", A.nrows, _ptr(A.rowptr), _ptr(out), _stream(A.rowptr.device))
+    return out
+
+
+def csr_spmm_scaled(A: CSR, rowscale: torch.Tensor | None, colscale: torch.Tensor | None, B: torch.Tensor,
+                    out: torch.Tensor | None = None, workspace: SpmmWorkspace | None = None) -> torch.Tensor:
+    """C[r] = rowscale[r] * sum over A's stored entries (r, c) of
+    colscale[c] * B[c] (A's values are not used; None = all ones)."""
+    A.validate_layout()
+    _check_cuda("B", B, tuple(_DT))
+    for name, t, n in (("rowscale", rowscale, A.nrows), ("colscale", colscale, A.ncols)):
+        if t is not None:
+            _check_cuda(name, t, torch.float32)
+            if t.numel() != n:
+                raise ValueError(f"{name} must have {n} entries")
+    F = int(B.shape[1])
+    if out is None:
+        out = torch.empty((A.nrows, F), dtype=torch.float32, device=B.device)
+    ws = workspace or SpmmWorkspace()
+    buf = ws.get(spmm_workspace_bytes(A.nrows, A.nnz, F, B.dtype), B.device)
+    _lib.call("gbs_csr_spmm_scaled", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind), _ptr(rowscale),
+              _ptr(colscale), _ptr(B), _DT[B.dtype], F, _ptr(out), _ptr(buf), buf.numel(), _stream(B.device))
+    return out
+
+
 class SpmmPlan:
     """Column-partitioned SpMM plan for a fixed A, feature width and type
-    (parts = 0 lets the library choose from B's size against L2)."""
+    (parts = 0 lets the library choose from B's size against L2).  With
+    rowscale / colscale the plan computes the degree-normalised product of
+    csr_spmm_scaled (A's values unused)."""
 
-    def __init__(self, A: CSR, F: int, dtype: torch.dtype = torch.float32, parts: int = 0):
+    def __init__(self, A: CSR, F: int, dtype: torch.dtype = torch.float32, parts: int = 0,
+                 rowscale: torch.Tensor | None = None, colscale: torch.Tensor | None = None):
         A.validate_layout()
         self.A, self.F, self.dtype = A, F, dtype
         h = C.c_void_p()
-        _lib.call("gbs_csr_spmm_plan_create", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
-                  _ptr(A.vals), _DT[dtype], F, parts, _stream(A.rowptr.device), C.byref(h))
+        if rowscale is not None or colscale is not None:
+            _lib.call("gbs_csr_spmm_plan_create_scaled", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr),
+                      _ptr(A.colind), _ptr(rowscale), _ptr(colscale), _DT[dtype], F, parts,
+                      _stream(A.rowptr.device), C.byref(h))
+        else:
+            _lib.call("gbs_csr_spmm_plan_create", A.nrows, A.ncols, A.nnz, _ptr(A.rowptr), _ptr(A.colind),
+                      _ptr(A.vals), _DT[dtype], F, parts, _stream(A.rowptr.device), C.byref(h))
         self._h = h
         k = C.c_int(0)
         _lib.call("gbs_csr_spmm_plan_parts", h, C.byref(k))
@@ -347,6 +385,17 @@ def bmm32_bin(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, m: int, n: int
     """Mirror of BMM32_BIN (or BMM32S_BIN with s_layout=True)."""
     _lib.call("gbs_bmm32s_bin" if s_layout else "gbs_bmm32_bin", _ptr(A), _ptr(B), _ptr(C_), m, n, k,
               _stream(A.device))
+
+
+BIN_FUSED, BIN_COUNTS = 0, 1
+
+
+def bmm_bin(A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor, m: int, n: int, k: int,
+            s_layout: bool = False, algo: int = BIN_FUSED) -> None:
+    """Sign words of the binary GEMM in the BMM32_BIN (or BMM32S_BIN) layout
+    with the algorithm chosen: BIN_FUSED thresholds in the tcgen05 epilogue,
+    BIN_COUNTS writes int32 counts first and packs them in a second pass."""
+    _lib.call("gbs_bmm_bin", _ptr(A), _ptr(B), _ptr(C_), m, n, k, int(s_layout), algo, _stream(A.device))
 
 
 # ---------------------------------------------------------------------------

@@ -69,6 +69,55 @@ def test_bmm32_bin_layouts(cuda, s_layout):
     assert np.array_equal(C.cpu().numpy().view(np.uint32), want)
 
 
+@pytest.mark.parametrize("s_layout", [False, True])
+@pytest.mark.parametrize("m, k, nbits", [(32, 32, 1), (96, 64, 153), (256, 512, 1024), (416, 288, 33),
+                                         (1024, 2080, 4096)])
+def test_bin_fused_epilogue_vs_counts_and_oracle(cuda, s_layout, m, k, nbits):
+    """Sign words thresholded in the tcgen05 epilogue equal the two-pass
+    form (int32 counts, then sign words) and the oracle, at sizes with
+    partial output tiles and n not a multiple of 32."""
+    rng = np.random.default_rng(m + k + nbits)
+    Kw = (nbits + 31) // 32
+    A, B = words(rng, Kw, m), words(rng, Kw, k)
+    dA, dB = torch.from_numpy(A.view(np.int32)).to(cuda), torch.from_numpy(B.view(np.int32)).to(cuda)
+    size = m * k if s_layout else (k // 32) * m
+    fused = torch.full((size,), 7, dtype=torch.int32, device=cuda)
+    two = torch.full((size,), 7, dtype=torch.int32, device=cuda)
+    ops.bmm_bin(dA, dB, fused, m, nbits, k, s_layout, ops.BIN_FUSED)
+    ops.bmm_bin(dA, dB, two, m, nbits, k, s_layout, ops.BIN_COUNTS)
+    assert torch.equal(fused, two)
+    want = (oracle.bmm32s_bin if s_layout else oracle.bmm32_bin)(A, B, m, nbits, k)
+    got = fused.cpu().numpy().view(np.uint32)
+    if s_layout:  # the reference's S layout writes k of every k * 32 words
+        used = (np.arange(m * k) % (k * 32)) < k
+        assert np.array_equal(got[used], want[used])
+        assert np.all(got[~used] == 7)
+    else:
+        assert np.array_equal(got, want)
+    assert ops.bmm_tc_timeouts() == 0
+
+
+def test_bin_fused_8192(cuda):
+    """The 8192 x 8192 x 8192-bit configuration: fused sign words equal the
+    two-pass form over the whole output, and the oracle on a sampled block."""
+    m = k = nbits = 8192
+    Kw = nbits // 32
+    rng = np.random.default_rng(8193)
+    A, B = words(rng, Kw, m), words(rng, Kw, k)
+    dA, dB = torch.from_numpy(A.view(np.int32)).to(cuda), torch.from_numpy(B.view(np.int32)).to(cuda)
+    fused = torch.zeros((k // 32) * m, dtype=torch.int32, device=cuda)
+    two = torch.zeros_like(fused)
+    ops.bmm_bin(dA, dB, fused, m, nbits, k, False, ops.BIN_FUSED)
+    ops.bmm_bin(dA, dB, two, m, nbits, k, False, ops.BIN_COUNTS)
+    assert torch.equal(fused, two)
+    r0, c0 = 4096, 8192 - 256
+    sub = oracle.bmm32_bin(np.ascontiguousarray(A[:, r0:r0 + 256]), np.ascontiguousarray(B[:, c0:c0 + 256]),
+                           256, nbits, 256)  # words [by][r] of the 256 x 256 block
+    got = fused.reshape(k // 32, m)[c0 // 32:(c0 + 256) // 32, r0:r0 + 256].cpu().numpy().view(np.uint32)
+    assert np.array_equal(got.reshape(-1), sub)
+    assert ops.bmm_tc_timeouts() == 0
+
+
 def test_sign_packed_dense_operands(cuda):
     """End to end from dense +-1 matrices: pack with ToBit32ColUd semantics,
     multiply, compare with the float product."""
