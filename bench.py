@@ -373,12 +373,18 @@ def other_configs(dev, timed, reps):
         fl["b2sr_spmm_f256_ms"][str(ts)] = round(mean_ms(timed, lambda: ops.b2sr_spmm(Ab, B, out=C), reps,
                                                          f"flickr_b2sr_{ts}"), 4)
         fl.setdefault("nnzb", {})[str(ts)] = Ab.nnzb
-        bm = {}
+        bm, bal = {}, {}
+        al = ops.b2sr_aligned(Ab) if ts in (8, 16) else None
         for F in (32, 64, 128, 256, 512, 1024):
             X = G.normal(F + 1, 8, (n, F), device=dev)
             Xw = ops.pack_sign_rows(X)
             bm[str(F)] = round(mean_ms(timed, lambda: ops.b2sr_bmm(Ab, Xw, F), reps, f"flickr_bmm_{ts}_{F}"), 4)
+            if al is not None:
+                bal[str(F)] = round(mean_ms(timed, lambda: ops.b2sr_bmm_aligned(Ab, al, Xw, F), reps,
+                                            f"flickr_bmm_aligned_{ts}_{F}"), 4)
         fl["bmm_ms"][str(ts)] = bm
+        if bal:
+            fl.setdefault("bmm_aligned_ms", {})[str(ts)] = bal
     out["flickr_like"] = fl
 
     # binary GEMM 8192 x 8192 x 8192 bits (default: persistent tcgen05)

@@ -153,7 +153,7 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
 /* Column-partitioned plan.  When B is larger than half of L2, splitting A by
  * column ranges into `parts` pieces (0 = choose: at least 2, then the
  * smallest power of two <= 8 whose B slice fits in L2; 1 when B fits in half
- * of L2 or rows of B are reused fewer than 8 times) and accumulating one
+ * of L2 or rows of B are reused fewer than 64 times on average) and accumulating one
  * merge-path pass per piece keeps each pass's row gathers in L2 (232,965 x
  * 256 B on GB300: FP32 6.26 ms in one pass, 5.93 ms as 2 parts, 6.35 ms as
  * 4; BF16 3.71 ms -> 3.50 ms as 2 parts).  The
@@ -352,9 +352,13 @@ GBS_API gbs_status gbs_b2sr_pack_aligned(int tile, int nblockrows,
 
 /* ------------------------------------------------------------------------
  * B2SR x dense (binary A):  C = A01 * B, C FP32 nrows x F (every row
- * written).  Tile 4 adds in the order of spmm4_full_full_new2
- * (spmm.cu:877-956), so its result is bitwise the reference's for any FP32
- * B; other tiles add in column order (exact for integer-valued B).
+ * written).  Block-rows of more than 256 tiles (power-law hubs) are cut into
+ * segments summed by different warps and added into C with float atomics,
+ * so their FP32 sums may differ in the last bits between runs (exact for
+ * integer-valued B such as 0/1 and +-1); the other block-rows add in the
+ * order of spmm4_full_full_new2 (spmm.cu:877-956) at tile 4 and in column
+ * order at tiles 8/16/32.  gbs_spmm4_full_full keeps the reference's order
+ * everywhere (bitwise its result for any FP32 B).
  * ------------------------------------------------------------------------ */
 GBS_API gbs_status gbs_b2sr_spmm(int tile, int nrows, int nblockrows,
                          const int *d_bsr_rowptr, const int *d_bsr_colind,
@@ -376,6 +380,17 @@ GBS_API gbs_status gbs_b2sr_bmm(int tile, int nrows, int nblockrows,
                         const int *d_bsr_rowptr, const int *d_bsr_colind,
                         const void *d_bsr_val, const uint32_t *d_X, int F,
                         int signed_form, int32_t *d_C, gbs_stream_t stream);
+
+/* The same product on the aligned B2SR-8/16 arrays of gbs_b2sr_pack_aligned
+ * (new_rowptr, new_colind, new_val): the consumer the reference builds those
+ * formats for ("bsrbmv", named at csr2bsr_batch_bsrbmv.cu:1, not shipped).
+ * Each uint32 word holds one row of 4 (tile 8) / 2 (tile 16) consecutive
+ * tiles; padding tiles carry no bits.  Same int32 result as gbs_b2sr_bmm on
+ * the plain arrays. */
+GBS_API gbs_status gbs_b2sr_bmm_aligned(int tile, int nrows, int nblockrows,
+                                const int *d_new_rowptr, const int *d_new_colind,
+                                const uint32_t *d_new_val, const uint32_t *d_X, int F,
+                                int signed_form, int32_t *d_C, gbs_stream_t stream);
 
 /* Dense sign packing, bit = (x >= 0), first column in bit 31, elements
  * outside the matrix read as -1 (bit 0).

@@ -99,6 +99,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbs_bmm32_bin": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm32s_bin": (st, [p, p, p, i32, i32, i32, p]),
     "gbs_bmm_bin": (st, [p, p, p, i32, i32, i32, i32, i32, p]),
+    "gbs_b2sr_bmm_aligned": (st, [i32, i32, i32, p, p, p, p, i32, i32, p, p]),
 }
 
 

@@ -360,6 +360,22 @@ __device__ __forceinline__ uint32_t tile_row(const void *val, size_t t, int r) {
   return (uint32_t)__ldg(reinterpret_cast<const VT *>(val) + t * TS + r);
 }
 
+// Row r of tile t in the aligned B2SR-8/16 layout (packUchar2AlignedUnsigned /
+// packUshort2AlignedUnsigned): tiles in groups of g = 32 / TS per uint32 word,
+// word (t / g) * TS + r holds row r of the group's tiles, the first tile in
+// the most significant byte / half.  t indexes the padded tile list.
+template <int TS, bool AL>
+__device__ __forceinline__ uint32_t tile_row_any(const void *val, size_t t, int r) {
+  if constexpr (AL) {
+    static_assert(TS == 8 || TS == 16, "aligned B2SR exists for tiles 8 and 16");
+    constexpr int g = 32 / TS;
+    const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(val) + (t / g) * TS + r);
+    return (w >> (TS * (g - 1 - (int)(t % g)))) & ((1u << TS) - 1u);
+  } else {
+    return tile_row<TS>(val, t, r);
+  }
+}
+
 // One warp: block-row br, tile rows [grp * R, grp * R + R), feature chunks
 // chunk0 + [0, LPR * CH); U entries gathered per round.  The tiles are read
 // G groups (of 32 / TS tiles = 32 entries) at a time; the entries of a step
@@ -369,9 +385,11 @@ __device__ __forceinline__ uint32_t tile_row(const void *val, size_t t, int r) {
 // Entries are added in group order and, inside a group, in lane order, so
 // every output element is the same sequence of FP32 additions as a
 // one-group-at-a-time walk.  `list` holds 32 * G entries (col, row bits).
-template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G>
+// tb0 / te0 >= 0: walk only tiles [tb0, te0) of the block-row, and (ATOMIC)
+// add the sums into C with float atomics instead of storing them.
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G, bool ATOMIC = false>
 __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long br, int grp, int chunk0,
-                                               int lane, int2 *list) {
+                                               int lane, int2 *list, int tb0 = -1, int te0 = -1) {
   constexpr int NSUB = 32 / LPR;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;  // tile rows per warp
   constexpr int TPG = 32 / TS;                          // tiles per 32 entries
@@ -394,7 +412,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[k][c][q] = 0.f;
 
-  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = te0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
   const int j = REF_ORDER ? lane / TPG : lane % TS;
   const int l = REF_ORDER ? lane % TPG : lane / TS;
   // this lane's entry (feature row, row bits) in each of G groups
@@ -469,7 +487,17 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
     for (int c = 0; c < CH; ++c) {
       const int chunk = chunk0 + c * LPR + sl;
       if (chunk >= a.nvec) continue;
-      if (STORE_NZ) {
+      if constexpr (ATOMIC) {
+        if constexpr (VEC % 4 == 0) {
+#pragma unroll
+          for (int q = 0; q < VEC; q += 4)
+            atomicAdd(reinterpret_cast<float4 *>(dst + (size_t)chunk * VEC + q),
+                      make_float4(acc[k][c][q], acc[k][c][q + 1], acc[k][c][q + 2], acc[k][c][q + 3]));
+        } else {
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) atomicAdd(dst + (size_t)chunk * VEC + q, acc[k][c][q]);
+        }
+      } else if (STORE_NZ) {
 #pragma unroll
         for (int q = 0; q < VEC; ++q)
           if (acc[k][c][q] != 0.f) dst[(size_t)chunk * VEC + q] = acc[k][c][q];
@@ -527,6 +555,53 @@ __global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hubs(B2srSpmmArgs a) {
   }
 }
 
+// Order-free hub pass (gbs_b2sr_spmm, whose addition order is free: the
+// reference's order is kept only by the drop-in gbs_spmm4_full_full).  A hub
+// block-row is cut into at most kHubMaxSegs segments of at least
+// kHubSegTiles tiles; one warp per (hub, segment, tile row, feature slice)
+// sums its segment and adds the sums into C with vector float atomics, into
+// hub rows zeroed before the pass.  The hub's chain of dependent gather
+// rounds is cut by the number of segments.  Exact for integer-valued
+// features (0/1, +-1: every partial sum is an integer below 2^24); for other
+// features the FP32 sums may differ in their last bits from run to run.
+constexpr int kHubSegTiles = 64;
+constexpr int kHubMaxSegs = 64;
+template <int TS, int DT, int VEC>
+__global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long per_hub = (long long)kHubMaxSegs * TS * a.slices;
+  const long long items = (long long)__ldg(a.hubs) * per_hub;
+  __shared__ int2 lists[8][32 * 4];
+  for (long long it = gw; it < items; it += nw) {
+    const long long h = it / per_hub;
+    long long r = it % per_hub;
+    const int seg = (int)(r / ((long long)TS * a.slices));
+    r %= (long long)TS * a.slices;
+    const int row = (int)(r / a.slices), sl = (int)(r % a.slices);
+    const long long br = __ldg(a.hubs + 1 + h);
+    const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+    const int len = max(kHubSegTiles, (te - tb + kHubMaxSegs - 1) / kHubMaxSegs);
+    const int t0 = tb + seg * len;
+    if (t0 >= te) continue;  // warp-uniform
+    b2sr_block_row<TS, DT, VEC, 32, 1, 1, false, HUB_U, 4, true>(a, br, row, sl * HUB_CHUNKS, lane,
+                                                                   lists[threadIdx.x >> 5], t0, min(te, t0 + len));
+  }
+}
+
+// Zeroes the C rows of the hub block-rows (before the atomic hub pass).
+__global__ void k_zero_hub_rows(const int *__restrict__ hubs, int ts, int nrows, long long ldc, int F,
+                                float *__restrict__ C) {
+  const long long n = (long long)__ldg(hubs) * ts * F;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long h = i / ((long long)ts * F);
+    const int r = (int)((i / F) % ts), c = (int)(i % F);
+    const long long row = (long long)__ldg(hubs + 1 + h) * ts + r;
+    if (row < nrows) C[row * ldc + c] = 0.f;
+  }
+}
+
 // hubs[0] = number of block-rows with more than hub_min tiles, hubs[1..] =
 // their ids (any order: each output element is computed whole by one warp).
 __global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs) {
@@ -540,7 +615,8 @@ namespace {
 struct B2srVariant {
   const void *fn;
   int vec, lpr, ch, rows_per_warp, groups;
-  const void *hub_fn;  // hub pass (32-chunk slices), same tile size and type
+  const void *hub_fn;      // hub pass (32-chunk slices), same tile size and type
+  const void *hub_seg_fn;  // order-free segmented hub pass (null for the drop-in)
 };
 
 template <int TS, int DT, int VEC, int LPR, int CH, bool NZ>
@@ -551,7 +627,8 @@ B2srVariant mk_b2sr() {
   constexpr int RPS = (NSUB * RPS1 > TS) ? ((TS / NSUB) > 0 ? TS / NSUB : 1) : RPS1;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
   return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
-                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>};
+                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>,
+                     NZ ? nullptr : (const void *)&k_b2sr_spmm_hub_segs<TS, DT, VEC>};
 }
 
 template <int TS, int DT, int VEC, bool NZ>
@@ -654,9 +731,16 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
   DeviceInfo di;
   GBS_TRY(device_info(&di));
   void *args[] = {&a};
-  // enough warps that every (hub, group, slice) item of a typical graph gets
-  // its own warp (surplus warps exit at once)
-  GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
+  if (v.hub_seg_fn) {
+    // order-free: zero the hub rows, then segments add into them
+    k_zero_hub_rows<<<di.sm_count * 4, 256, 0, side>>>(a.hubs, ts, nrows, a.ldc, F, C);
+    GBS_TRY(check_launch("k_zero_hub_rows"));
+    GBS_CUDA_TRY(cudaLaunchKernel(v.hub_seg_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
+  } else {
+    // enough warps that every (hub, group, slice) item of a typical graph
+    // gets its own warp (surplus warps exit at once)
+    GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
+  }
   GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
   gbs_status st = GBS_OK;
   cudaError_t e = cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s);
@@ -691,7 +775,9 @@ struct B2srBmmArgs {
 // groups at a time are compacted into the per-warp shared-memory list (as
 // in b2sr_block_row), then gathered U at a time while the next step's
 // indices load.  Integer counts: the order of entries does not matter here.
-template <int TS, int WMAX, int R, int U, int G>
+// AL: the tiles come in the aligned B2SR-8/16 layout (padding tiles carry
+// no bits, so they drop out at the compaction).
+template <int TS, int WMAX, int R, int U, int G, bool AL>
 __device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br, int grp, int lane, int2 *list) {
   constexpr int TPG = 32 / TS;
   constexpr int TPS = TPG * G;
@@ -720,7 +806,8 @@ __device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br
         nb[g] = __ldg(a.colind + t) * TS + j;
 #pragma unroll
         for (int i = 0; i < R; ++i)
-          if (row0 + i < TS) nm[g] |= ((tile_row<TS>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
+          if (row0 + i < TS)
+            nm[g] |= ((tile_row_any<TS, AL>(a.val, (size_t)t, row0 + i) >> (TS - 1 - j)) & 1u) << i;
       }
     }
   };
@@ -782,7 +869,7 @@ struct BmmShape {
 
 // Main pass: one warp per (block-row, group of R rows), R * WMAX <= 32
 // counters per lane.
-template <int TS, int WMAX>
+template <int TS, int WMAX, bool AL>
 __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
   constexpr int R = BmmShape<WMAX>::R0 < TS ? BmmShape<WMAX>::R0 : TS;
   constexpr int NG = (TS + R - 1) / R;
@@ -792,7 +879,7 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
   if (br >= a.mb) return;
   if (a.hub_min > 0 && __ldg(a.rowptr + br + 1) - __ldg(a.rowptr + br) > a.hub_min) return;
   __shared__ int2 lists[8][32 * 2];
-  bmm_block_row<TS, WMAX, R, BmmShape<WMAX>::U, 2>(a, br, (int)(gw % NG), lane, lists[threadIdx.x >> 5]);
+  bmm_block_row<TS, WMAX, R, BmmShape<WMAX>::U, 2, AL>(a, br, (int)(gw % NG), lane, lists[threadIdx.x >> 5]);
 }
 
 // One warp, one tile row `row` of a hub block-row.  The entries of 4 groups
@@ -802,7 +889,7 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
 // WMAX loads per lane and no more registers -- and each word is broadcast to
 // the lanes by a shuffle when its bits are counted.  The chain of dependent
 // round trips is (entries / 32) deep instead of (entries / U).
-template <int TS, int WMAX>
+template <int TS, int WMAX, bool AL>
 __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list) {
   constexpr int G = 4;
   constexpr int TPG = 32 / TS;
@@ -826,7 +913,7 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
       bool set = false;
       if (t < te) {
         col = __ldg(a.colind + t) * TS + j;
-        set = (tile_row<TS>(a.val, (size_t)t, row) >> (TS - 1 - j)) & 1u;
+        set = (tile_row_any<TS, AL>(a.val, (size_t)t, row) >> (TS - 1 - j)) & 1u;
       }
       const unsigned act = __ballot_sync(0xffffffffu, set);
       if (set) list[n + __popc(act & lt_mask)] = make_int2(col, 0);
@@ -865,7 +952,7 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
 }
 
 // Hub pass: one warp per (hub block-row, tile row), items grid-stride.
-template <int TS, int WMAX>
+template <int TS, int WMAX, bool AL>
 __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
   const int lane = threadIdx.x & 31;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -874,18 +961,18 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
   __shared__ int2 lists[8][32 * 4];
   for (long long it = gw; it < items; it += nw) {
     const long long br = __ldg(a.hubs + 1 + it / TS);
-    bmm_hub_row<TS, WMAX>(a, br, (int)(it % TS), lane, lists[threadIdx.x >> 5]);
+    bmm_hub_row<TS, WMAX, AL>(a, br, (int)(it % TS), lane, lists[threadIdx.x >> 5]);
   }
 }
 
-template <int TS>
+template <int TS, bool AL = false>
 gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   const void *fn = nullptr, *hub_fn = nullptr;
   int wmax = 0;
 #define GBS_BMM_CASE(WM)                                 \
   {                                                      \
-    fn = (const void *)&k_b2sr_bmm<TS, WM>;              \
-    hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM>;     \
+    fn = (const void *)&k_b2sr_bmm<TS, WM, AL>;          \
+    hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM, AL>; \
     wmax = WM;                                           \
   }
   if (a.W <= 1) GBS_BMM_CASE(1)
@@ -1129,6 +1216,30 @@ extern "C" gbs_status gbs_b2sr_bmm(int tile, int nrows, int nblockrows, const in
     case 16: return launch_bmm<16>(a, s);
     default: return launch_bmm<32>(a, s);
   }
+}
+
+extern "C" gbs_status gbs_b2sr_bmm_aligned(int tile, int nrows, int nblockrows, const int *new_rowptr,
+                                           const int *new_colind, const uint32_t *new_val, const uint32_t *X,
+                                           int F, int signed_form, int32_t *C, gbs_stream_t stream) {
+  clear_error();
+  GBS_REQUIRE(tile == 8 || tile == 16, "b2sr bmm aligned: tile must be 8 or 16");
+  GBS_REQUIRE(nrows >= 0 && F >= 1 && F <= 1024, "b2sr bmm aligned: need 1 <= F <= 1024");
+  GBS_REQUIRE(nblockrows == (nrows + tile - 1) / tile, "b2sr bmm aligned: nblockrows must be ceil(nrows / tile)");
+  if (nrows == 0) return GBS_OK;
+  GBS_REQUIRE(new_rowptr && C && X, "b2sr bmm aligned: null pointer");
+  B2srBmmArgs a;
+  a.nrows = nrows;
+  a.mb = nblockrows;
+  a.F = F;
+  a.W = (F + 31) / 32;
+  a.rowptr = new_rowptr;
+  a.colind = new_colind;
+  a.val = new_val;
+  a.X = X;
+  a.C = C;
+  a.signed_form = signed_form ? 1 : 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  return tile == 8 ? launch_bmm<8, true>(a, s) : launch_bmm<16, true>(a, s);
 }
 
 extern "C" gbs_status gbs_b2sr_aligned_nnzb(int tile, int nblockrows, const int *bsr_rowptr, int *new_rowptr,

@@ -39,12 +39,9 @@ template <int DT, int VEC, int LPR, int CH>
 SpmmVariant mkb() {
   constexpr int UCAP = CH == 1 ? 4 : (CH == 2 ? 2 : 1);
   constexpr int U = UCAP < LPR ? UCAP : LPR;
-  // accumulators + blocked partials + H row + loads in flight.  16-bit
-  // features skip the blocked partials but keep this estimate: capped at 64
-  // registers (4 CTAs per SM) the BF16 backward of the 114.8M-edge graph at
-  // F = 256 measured 8.60 against 8.22 ms at 3 CTAs.
-  constexpr int EST = 24 + 3 * CH * VEC + U * CH * 4 + 2 * U;
-  constexpr int MINB = EST <= 64 ? 4 : (EST <= 80 ? 3 : (EST <= 128 ? 2 : 1));
+  // accumulators (+ blocked partials, FP32 only) + H row + loads in flight
+  constexpr int EST = 24 + (DT == DT_F32 ? 3 : 2) * CH * VEC + U * CH * 4 + 2 * U;
+  constexpr int MINB = EST <= 60 ? 4 : (EST <= 80 ? 3 : (EST <= 128 ? 2 : 1));
   return SpmmVariant{(const void *)&k_csr_spmm_bwd<DT, VEC, LPR, CH, U, MINB>, VEC, LPR, CH};
 }
 
@@ -55,6 +52,13 @@ bool pickb(int nvec, SpmmVariant *v) {
   if (nvec <= 4) { *v = mkb<DT, VEC, 4, 1>(); return true; }
   if (nvec <= 8) { *v = mkb<DT, VEC, 8, 1>(); return true; }
   if (nvec <= 16) { *v = mkb<DT, VEC, 16, 1>(); return true; }
+  // 16-bit rows of 17-32 chunks (F = 136..256) on half-warps: one shuffle
+  // pair and one dot-product butterfly serve two gathers per lane (BF16
+  // backward step of the 114.8M-edge graph at F = 256: 6.69 against 7.66 ms
+  // on full-warp rows)
+  if constexpr (VEC == 8) {
+    if (nvec <= 32) { *v = mkb<DT, VEC, 16, 2>(); return true; }
+  }
   if (nvec <= 32) { *v = mkb<DT, VEC, 32, 1>(); return true; }
   if (nvec <= 64) { *v = mkb<DT, VEC, 32, 2>(); return true; }
   if (nvec <= 128) { *v = mkb<DT, VEC, 32, 4>(); return true; }

@@ -75,17 +75,33 @@ struct MergeKernel {
   // n_valid (their loads are skipped and their values zeroed); otherwise
   // every entry exists and the loads go out unpredicated.  Lanes whose chunk
   // lies past the row gather the row's last chunk; their sums are never
-  // stored.
+  // stored.  The (column, value) pairs come from the warp's batch staged in
+  // shared memory sub-group-major, so one 16-byte load gives a sub-group two
+  // entries where two shuffles per entry broadcast them before (114.8M-edge
+  // graph, F = 256: FP32 5.81 against 5.92 ms, BF16 3.35 against 3.46 ms;
+  // in the fused backward the same staging measured slower, 6.10 against
+  // 6.00 ms, so it keeps the shuffles).
   template <bool TAIL>
   static __device__ __forceinline__ void round(const MergeArgs &a, int u0, int n_valid, int sub, int sl,
-                                               int my_col, float my_val, float (&bs)[CH][VEC]) {
+                                               const int2 *stage, float (&bs)[CH][VEC]) {
     raw bv[U][CH];
     float vv[U];
+    int2 ent[U];
+    if constexpr (U % 2 == 0) {
+#pragma unroll
+      for (int u = 0; u < U; u += 2) {
+        const int4 q = *reinterpret_cast<const int4 *>(stage + sub * (32 / NSUB) + ((u0 + u) & (32 / NSUB - 1)));
+        ent[u] = make_int2(q.x, q.y);
+        ent[u + 1] = make_int2(q.z, q.w);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u) ent[u] = stage[sub * (32 / NSUB) + ((u0 + u) & (32 / NSUB - 1))];
+    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int k = ((u0 + u) * NSUB + sub) & 31;
-      const int col = __shfl_sync(0xffffffffu, my_col, k);
-      const float v = __shfl_sync(0xffffffffu, my_val, k);
+      const int col = ent[u].x;
+      const float v = __int_as_float(ent[u].y);
       const bool ok = !TAIL || (u0 + u) * NSUB + sub < n_valid;
       vv[u] = ok ? v : 0.f;
       // 32 x 32 -> 64-bit row offset (row strides are checked below 2^32 bytes)
@@ -134,16 +150,22 @@ struct MergeKernel {
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[c][q] = 0.f;
 
-    // fused backward addressing: row col of B starts at lane_b + col * pitch
-    // bytes for this lane's first chunk (one 32 x 32 -> 64-bit multiply-add
-    // per gather), chunk c lies c * LPR * VEC elements further; in_row[c]
-    // is the lane's round-invariant guard (BF16 7.51 against 8.12 ms, FP32
-    // 9.64 against 10.02 ms per backward step of the 114.8M-edge graph)
-    const char *lane_b = static_cast<const char *>(a.B) + (size_t)sl * VEC * sizeof(typename F_::storage_t);
-    const unsigned pitch = (unsigned)(a.ldb * (long long)sizeof(typename F_::storage_t));
-    bool in_row[CH];
+    // fused backward addressing: chunk c of row col of B starts at
+    // lane_b[c] + col * pitch bytes (one 32 x 32 -> 64-bit multiply-add per
+    // gathered chunk).  A lane whose chunk lies past the row reads the row's
+    // last chunk instead, so every gather is an unconditional in-bounds load:
+    // its FMAs land in accumulator slots that are never stored and its
+    // dot-product terms meet a zero H element.  Entries past the end of a
+    // batch gather the row of a column the lane held before (a valid row)
+    // with weight 0, and their dot products are not stored.  (Predicated
+    // loads with zero fill measured 9.61 / 7.66 ms against 8.82 / 6.83 ms
+    // per FP32 / BF16 backward step of the 114.8M-edge graph.)
+    const char *lane_b[CH];
 #pragma unroll
-    for (int c = 0; c < CH; ++c) in_row[c] = c * LPR + sl < a.nvec;
+    for (int c = 0; c < CH; ++c)
+      lane_b[c] = static_cast<const char *>(a.B) +
+                  (size_t)min(c * LPR + sl, a.nvec - 1) * VEC * sizeof(typename F_::storage_t);
+    const unsigned pitch = (unsigned)(a.ldb * (long long)sizeof(typename F_::storage_t));
     raw bv[U][CH];
 #pragma unroll
     for (int u = 0; u < U; ++u)
@@ -179,8 +201,9 @@ struct MergeKernel {
       // unrolled loop with early exits) keeps the loads of one round
       // together.  Only the last round of a batch can hold missing entries:
       // the forward runs the others unpredicated (BF16 3.66 against 4.21 ms,
-      // 114.8M-edge graph, F = 256), while the fused backward keeps one
-      // predicated loop (split, it measured 10.9 against 10.0 ms in FP32).
+      // 114.8M-edge graph, F = 256); the fused backward runs one loop of
+      // unconditional loads with zero weights past the batch (a split into
+      // full rounds and a tail measured 10.9 against 10.0 ms in FP32).
       if constexpr (SD) {
         const int rounds = (n_valid + U * NSUB - 1) / (U * NSUB);
 #pragma unroll 1
@@ -194,12 +217,9 @@ struct MergeKernel {
             const float v = __shfl_sync(0xffffffffu, my_val, k);
             const bool ok = (u0 + u) * NSUB + sub < n_valid;
             vv[u] = ok ? v : 0.f;
-            const char *p = lane_b + (size_t)(unsigned)col * pitch;
+            const size_t rowoff = (size_t)(unsigned)col * pitch;
 #pragma unroll
-            for (int c = 0; c < CH; ++c) {
-              if (ok && in_row[c]) bv[u][c] = F_::load(p, (size_t)c * LPR * VEC);
-              else bv[u][c] = F_::zero();
-            }
+            for (int c = 0; c < CH; ++c) bv[u][c] = F_::load(lane_b[c] + rowoff, 0);
           }
           // each gathered chunk is widened once and feeds both the row sum
           // and the dot product with the H row (even / odd columns as the
@@ -231,10 +251,16 @@ struct MergeKernel {
           sddmm_reduce(a, base, u0, n_valid, sub, sl, sd);
         }
       } else {
+        // stage the batch: entry k at position (k % NSUB) * (32 / NSUB) + k / NSUB
+        __shared__ __align__(16) int2 fstage_all[8][32];
+        int2 *stage = fstage_all[threadIdx.x >> 5];
+        __syncwarp();
+        stage[(lane % NSUB) * (32 / NSUB) + lane / NSUB] = make_int2(my_col, __float_as_int(my_val));
+        __syncwarp();
         const int full = n_valid / (U * NSUB);
 #pragma unroll 1
-        for (int rd = 0; rd < full; ++rd) round<false>(a, rd * U, n_valid, sub, sl, my_col, my_val, bs);
-        if (full * U * NSUB < n_valid) round<true>(a, full * U, n_valid, sub, sl, my_col, my_val, bs);
+        for (int rd = 0; rd < full; ++rd) round<false>(a, rd * U, n_valid, sub, sl, stage, bs);
+        if (full * U * NSUB < n_valid) round<true>(a, full * U, n_valid, sub, sl, stage, bs);
       }
       if constexpr (BLK) {
 #pragma unroll

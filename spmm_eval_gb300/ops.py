@@ -270,8 +270,9 @@ def csr2b2sr(A: CSR, tile: int) -> B2SR:
 
 
 def b2sr_spmm(Ab: B2SR, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-    """C = A01 @ B (FP32 out).  Tile 4 reproduces spmm4_full_full_new2's
-    addition order exactly."""
+    """C = A01 @ B (FP32 out).  Hub block-rows (> 256 tiles) are summed in
+    segments that meet through float atomics (exact for integer-valued B);
+    spmm4_full_full keeps the reference's addition order everywhere."""
     _check_cuda("B", B, tuple(_DT))
     F = int(B.shape[1])
     if out is None:
@@ -327,6 +328,17 @@ def b2sr_bmm(Ab: B2SR, Xbits: torch.Tensor, F: int, signed_form: bool = False) -
     out = torch.empty((Ab.nrows, F), dtype=torch.int32, device=Xbits.device)
     _lib.call("gbs_b2sr_bmm", Ab.tile, Ab.nrows, Ab.nblockrows, _ptr(Ab.rowptr), _ptr(Ab.colind),
               _ptr(Ab.val), _ptr(Xbits), F, int(signed_form), _ptr(out), _stream(Xbits.device))
+    return out
+
+
+def b2sr_bmm_aligned(Ab: B2SR, aligned, Xbits: torch.Tensor, F: int, signed_form: bool = False) -> torch.Tensor:
+    """b2sr_bmm on the aligned arrays (rowptr, colind, words) that
+    b2sr_aligned(Ab) returns (tile 8 or 16)."""
+    _check_cuda("Xbits", Xbits, torch.int32)
+    nrp, ncol, nval = aligned
+    out = torch.empty((Ab.nrows, F), dtype=torch.int32, device=Xbits.device)
+    _lib.call("gbs_b2sr_bmm_aligned", Ab.tile, Ab.nrows, Ab.nblockrows, _ptr(nrp), _ptr(ncol), _ptr(nval),
+              _ptr(Xbits), F, int(signed_form), _ptr(out), _stream(Xbits.device))
     return out
 
 
