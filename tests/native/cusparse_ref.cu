@@ -71,3 +71,58 @@ extern "C" int ref_spmm_colmajor(int nrows, int ncols, int nnz, const int *rowpt
   cusparseDestroy(h);
   return st;
 }
+
+// Timing handle for the comparison script: the SpMM of ref_spmm_colmajor
+// (or with row-major B / C, order = 1) set up once -- handle, descriptors,
+// work buffer, preprocessing -- so that ref_spmm_handle_run issues only the
+// cusparseSpMM call, on the legacy default stream.
+struct RefSpmm {
+  cusparseHandle_t h;
+  cusparseSpMatDescr_t A;
+  cusparseDnMatDescr_t B, C;
+  void *buf;
+};
+
+extern "C" void *ref_spmm_handle_create(int nrows, int ncols, int nnz, const int *rowptr, const int *colind,
+                                        const float *vals, const float *B, int F, float *C, int order) {
+  RefSpmm *r = new RefSpmm();
+  float alpha = 1.f, beta = 0.f;
+  if (cusparseCreate(&r->h) != CUSPARSE_STATUS_SUCCESS) { delete r; return nullptr; }
+  cusparseCreateCsr(&r->A, nrows, ncols, nnz, (void *)rowptr, (void *)colind, (void *)vals, CUSPARSE_INDEX_32I,
+                    CUSPARSE_INDEX_32I, CUSPARSE_INDEX_BASE_ZERO, CUDA_R_32F);
+  if (order == 0) {
+    cusparseCreateDnMat(&r->B, ncols, F, ncols, (void *)B, CUDA_R_32F, CUSPARSE_ORDER_COL);
+    cusparseCreateDnMat(&r->C, nrows, F, nrows, (void *)C, CUDA_R_32F, CUSPARSE_ORDER_COL);
+  } else {
+    cusparseCreateDnMat(&r->B, ncols, F, F, (void *)B, CUDA_R_32F, CUSPARSE_ORDER_ROW);
+    cusparseCreateDnMat(&r->C, nrows, F, F, (void *)C, CUDA_R_32F, CUSPARSE_ORDER_ROW);
+  }
+  size_t sz = 0;
+  cusparseSpMM_bufferSize(r->h, CUSPARSE_OPERATION_NON_TRANSPOSE, CUSPARSE_OPERATION_NON_TRANSPOSE, &alpha, r->A,
+                          r->B, &beta, r->C, CUDA_R_32F, CUSPARSE_SPMM_ALG_DEFAULT, &sz);
+  r->buf = nullptr;
+  if (sz) cudaMalloc(&r->buf, sz);
+  cusparseSpMM_preprocess(r->h, CUSPARSE_OPERATION_NON_TRANSPOSE, CUSPARSE_OPERATION_NON_TRANSPOSE, &alpha, r->A,
+                          r->B, &beta, r->C, CUDA_R_32F, CUSPARSE_SPMM_ALG_DEFAULT, r->buf);
+  cudaDeviceSynchronize();
+  return r;
+}
+
+extern "C" int ref_spmm_handle_run(void *p) {
+  RefSpmm *r = static_cast<RefSpmm *>(p);
+  float alpha = 1.f, beta = 0.f;
+  return (int)cusparseSpMM(r->h, CUSPARSE_OPERATION_NON_TRANSPOSE, CUSPARSE_OPERATION_NON_TRANSPOSE, &alpha, r->A,
+                           r->B, &beta, r->C, CUDA_R_32F, CUSPARSE_SPMM_ALG_DEFAULT, r->buf);
+}
+
+extern "C" void ref_spmm_handle_destroy(void *p) {
+  RefSpmm *r = static_cast<RefSpmm *>(p);
+  if (!r) return;
+  cudaDeviceSynchronize();
+  if (r->buf) cudaFree(r->buf);
+  cusparseDestroySpMat(r->A);
+  cusparseDestroyDnMat(r->B);
+  cusparseDestroyDnMat(r->C);
+  cusparseDestroy(r->h);
+  delete r;
+}
