@@ -676,7 +676,8 @@ def run_profile_case(args):
       l2resident : 232,965 rows x 492 nonzeros, columns uniform over 8K / 32K /
                128K rows (B in L2), planned FP32 and BF16 SpMM, event-timed
                medians printed (not an ncu case)
-      b2sr   : flickr-shaped graph, CSR->B2SR-4 packing, FBF SpMM F = 256,
+      b2sr   : flickr-shaped graph, for tiles 4 / 8 / 16 / 32: CSR->B2SR
+               packing, B2SR SpMM F = 256 (tile 4 also the ordered drop-in),
                B2SR BMM F = 256
       bmm    : 4096^3 binary GEMM, popc, mma .b1, tcgen05 per tile, tcgen05
                persistent (XOR counts)
@@ -762,13 +763,19 @@ def run_profile_case(args):
         A = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
         B = G.normal(3, 3, (g.ncols, 256), device=dev)
         Xw = ops.pack_sign_rows(B)
-        for _ in range(2 + args.steps):
-            Ab = ops.csr2b2sr(A, 4)
-        for _ in range(2 + args.steps):
-            ops.b2sr_spmm(Ab, B)
-        for _ in range(2 + args.steps):
-            ops.b2sr_bmm(Ab, Xw, 256)
-        out.update(nodes=g.nrows, nnz=g.nnz, nnzb=Ab.nnzb)
+        for ts in (4, 8, 16, 32):
+            for _ in range(2 + args.steps):
+                Ab = ops.csr2b2sr(A, ts)
+            for _ in range(2 + args.steps):
+                ops.b2sr_spmm(Ab, B)
+            if ts == 4:
+                Cd = torch.zeros((Ab.nblockrows * 4, 256), device=dev)
+                for _ in range(2 + args.steps):
+                    ops.spmm4_full_full(Ab.val, B, Cd, Ab.rowptr, Ab.colind, Ab.nblockrows, 256)
+            for _ in range(2 + args.steps):
+                ops.b2sr_bmm(Ab, Xw, 256)
+            out.setdefault("nnzb", {})[ts] = Ab.nnzb
+        out.update(nodes=g.nrows, nnz=g.nnz)
     elif case in ("bmm", "bmmtc"):
         gen = torch.Generator(device=dev)
         gen.manual_seed(0)

@@ -352,13 +352,9 @@ GBS_API gbs_status gbs_b2sr_pack_aligned(int tile, int nblockrows,
 
 /* ------------------------------------------------------------------------
  * B2SR x dense (binary A):  C = A01 * B, C FP32 nrows x F (every row
- * written).  Block-rows of more than 256 tiles (power-law hubs) are cut into
- * segments summed by different warps and added into C with float atomics,
- * so their FP32 sums may differ in the last bits between runs (exact for
- * integer-valued B such as 0/1 and +-1); the other block-rows add in the
- * order of spmm4_full_full_new2 (spmm.cu:877-956) at tile 4 and in column
- * order at tiles 8/16/32.  gbs_spmm4_full_full keeps the reference's order
- * everywhere (bitwise its result for any FP32 B).
+ * written).  Tile 4 adds in the order of spmm4_full_full_new2
+ * (spmm.cu:877-956), so its result is bitwise the reference's for any FP32
+ * B; other tiles add in column order (exact for integer-valued B).
  * ------------------------------------------------------------------------ */
 GBS_API gbs_status gbs_b2sr_spmm(int tile, int nrows, int nblockrows,
                          const int *d_bsr_rowptr, const int *d_bsr_colind,

@@ -385,11 +385,9 @@ __device__ __forceinline__ uint32_t tile_row_any(const void *val, size_t t, int 
 // Entries are added in group order and, inside a group, in lane order, so
 // every output element is the same sequence of FP32 additions as a
 // one-group-at-a-time walk.  `list` holds 32 * G entries (col, row bits).
-// tb0 / te0 >= 0: walk only tiles [tb0, te0) of the block-row, and (ATOMIC)
-// add the sums into C with float atomics instead of storing them.
-template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G, bool ATOMIC = false>
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G>
 __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long br, int grp, int chunk0,
-                                               int lane, int2 *list, int tb0 = -1, int te0 = -1) {
+                                               int lane, int2 *list) {
   constexpr int NSUB = 32 / LPR;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;  // tile rows per warp
   constexpr int TPG = 32 / TS;                          // tiles per 32 entries
@@ -412,7 +410,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[k][c][q] = 0.f;
 
-  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = te0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
   const int j = REF_ORDER ? lane / TPG : lane % TS;
   const int l = REF_ORDER ? lane % TPG : lane / TS;
   // this lane's entry (feature row, row bits) in each of G groups
@@ -487,17 +485,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
     for (int c = 0; c < CH; ++c) {
       const int chunk = chunk0 + c * LPR + sl;
       if (chunk >= a.nvec) continue;
-      if constexpr (ATOMIC) {
-        if constexpr (VEC % 4 == 0) {
-#pragma unroll
-          for (int q = 0; q < VEC; q += 4)
-            atomicAdd(reinterpret_cast<float4 *>(dst + (size_t)chunk * VEC + q),
-                      make_float4(acc[k][c][q], acc[k][c][q + 1], acc[k][c][q + 2], acc[k][c][q + 3]));
-        } else {
-#pragma unroll
-          for (int q = 0; q < VEC; ++q) atomicAdd(dst + (size_t)chunk * VEC + q, acc[k][c][q]);
-        }
-      } else if (STORE_NZ) {
+      if (STORE_NZ) {
 #pragma unroll
         for (int q = 0; q < VEC; ++q)
           if (acc[k][c][q] != 0.f) dst[(size_t)chunk * VEC + q] = acc[k][c][q];
@@ -555,53 +543,6 @@ __global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hubs(B2srSpmmArgs a) {
   }
 }
 
-// Order-free hub pass (gbs_b2sr_spmm, whose addition order is free: the
-// reference's order is kept only by the drop-in gbs_spmm4_full_full).  A hub
-// block-row is cut into at most kHubMaxSegs segments of at least
-// kHubSegTiles tiles; one warp per (hub, segment, tile row, feature slice)
-// sums its segment and adds the sums into C with vector float atomics, into
-// hub rows zeroed before the pass.  The hub's chain of dependent gather
-// rounds is cut by the number of segments.  Exact for integer-valued
-// features (0/1, +-1: every partial sum is an integer below 2^24); for other
-// features the FP32 sums may differ in their last bits from run to run.
-constexpr int kHubSegTiles = 64;
-constexpr int kHubMaxSegs = 64;
-template <int TS, int DT, int VEC>
-__global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
-  const int lane = threadIdx.x & 31;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long per_hub = (long long)kHubMaxSegs * TS * a.slices;
-  const long long items = (long long)__ldg(a.hubs) * per_hub;
-  __shared__ int2 lists[8][32 * 4];
-  for (long long it = gw; it < items; it += nw) {
-    const long long h = it / per_hub;
-    long long r = it % per_hub;
-    const int seg = (int)(r / ((long long)TS * a.slices));
-    r %= (long long)TS * a.slices;
-    const int row = (int)(r / a.slices), sl = (int)(r % a.slices);
-    const long long br = __ldg(a.hubs + 1 + h);
-    const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
-    const int len = max(kHubSegTiles, (te - tb + kHubMaxSegs - 1) / kHubMaxSegs);
-    const int t0 = tb + seg * len;
-    if (t0 >= te) continue;  // warp-uniform
-    b2sr_block_row<TS, DT, VEC, 32, 1, 1, false, HUB_U, 4, true>(a, br, row, sl * HUB_CHUNKS, lane,
-                                                                   lists[threadIdx.x >> 5], t0, min(te, t0 + len));
-  }
-}
-
-// Zeroes the C rows of the hub block-rows (before the atomic hub pass).
-__global__ void k_zero_hub_rows(const int *__restrict__ hubs, int ts, int nrows, long long ldc, int F,
-                                float *__restrict__ C) {
-  const long long n = (long long)__ldg(hubs) * ts * F;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const long long h = i / ((long long)ts * F);
-    const int r = (int)((i / F) % ts), c = (int)(i % F);
-    const long long row = (long long)__ldg(hubs + 1 + h) * ts + r;
-    if (row < nrows) C[row * ldc + c] = 0.f;
-  }
-}
-
 // hubs[0] = number of block-rows with more than hub_min tiles, hubs[1..] =
 // their ids (any order: each output element is computed whole by one warp).
 __global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs) {
@@ -615,8 +556,7 @@ namespace {
 struct B2srVariant {
   const void *fn;
   int vec, lpr, ch, rows_per_warp, groups;
-  const void *hub_fn;      // hub pass (32-chunk slices), same tile size and type
-  const void *hub_seg_fn;  // order-free segmented hub pass (null for the drop-in)
+  const void *hub_fn;  // hub pass (32-chunk slices), same tile size and type
 };
 
 template <int TS, int DT, int VEC, int LPR, int CH, bool NZ>
@@ -627,8 +567,7 @@ B2srVariant mk_b2sr() {
   constexpr int RPS = (NSUB * RPS1 > TS) ? ((TS / NSUB) > 0 ? TS / NSUB : 1) : RPS1;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
   return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
-                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>,
-                     NZ ? nullptr : (const void *)&k_b2sr_spmm_hub_segs<TS, DT, VEC>};
+                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>};
 }
 
 template <int TS, int DT, int VEC, bool NZ>
@@ -731,16 +670,9 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
   DeviceInfo di;
   GBS_TRY(device_info(&di));
   void *args[] = {&a};
-  if (v.hub_seg_fn) {
-    // order-free: zero the hub rows, then segments add into them
-    k_zero_hub_rows<<<di.sm_count * 4, 256, 0, side>>>(a.hubs, ts, nrows, a.ldc, F, C);
-    GBS_TRY(check_launch("k_zero_hub_rows"));
-    GBS_CUDA_TRY(cudaLaunchKernel(v.hub_seg_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
-  } else {
-    // enough warps that every (hub, group, slice) item of a typical graph
-    // gets its own warp (surplus warps exit at once)
-    GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
-  }
+  // enough warps that every (hub, group, slice) item of a typical graph gets
+  // its own warp (surplus warps exit at once)
+  GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
   GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
   gbs_status st = GBS_OK;
   cudaError_t e = cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s);

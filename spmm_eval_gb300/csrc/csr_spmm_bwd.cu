@@ -282,12 +282,46 @@ extern "C" gbs_status gbs_spmm_backward_planned(const gbs_spmm_backward_plan *P,
   cudaStream_t s = (cudaStream_t)stream;
   DevBuf tmp;
   GBS_TRY(tmp.alloc(sizeof(float) * (size_t)P->nnz, s));
-  for (int p = 0; p < cp.K; ++p)
+  // Part p holds the entries of a range of A's rows, so A's entries
+  // [off_p, off_p + nnz_p) take their dvals from part p's block of the
+  // temporary only: part p's gather runs on the side stream while the next
+  // pass runs, and only the last part's gather follows the passes.
+  cudaStream_t side = nullptr;
+  if (cp.K > 1) GBS_TRY(side_stream(&side));
+  std::vector<cudaEvent_t> evs;
+  struct EvGuard {
+    std::vector<cudaEvent_t> &e;
+    ~EvGuard() {
+      for (auto x : e) cudaEventDestroy(x);
+    }
+  } guard{evs};
+  auto gather = [&](int p, cudaStream_t st) -> gbs_status {
+    const int m = cp.nnz[p];
+    if (m == 0) return GBS_OK;
+    const long long o = P->off[p];
+    k_gather_dvals<<<(int)(((long long)m + 255) / 256), 256, 0, st>>>(P->q + o, tmp.as<float>(), m, dvals + o);
+    return check_launch("k_gather_dvals");
+  };
+  for (int p = 0; p < cp.K; ++p) {
     GBS_TRY(bwd_launch(v, P->n, cp.nnz[p], cp.rowptr[p], cp.colind[p], cp.vals[p], nullptr, dC, H, P->F, dB,
                        tmp.as<float>() + P->off[p], ws, ws_bytes, p > 0 ? 1 : 0, s));
-  if (P->nnz > 0) {
-    k_gather_dvals<<<(int)(((long long)P->nnz + 255) / 256), 256, 0, s>>>(P->q, tmp.as<float>(), P->nnz, dvals);
-    GBS_TRY(check_launch("k_gather_dvals"));
+    if (p + 1 < cp.K) {
+      cudaEvent_t e = nullptr;
+      GBS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      evs.push_back(e);
+      GBS_CUDA_TRY(cudaEventRecord(e, s));
+      GBS_CUDA_TRY(cudaStreamWaitEvent(side, e, 0));
+      GBS_TRY(gather(p, side));
+    } else {
+      GBS_TRY(gather(p, s));
+    }
+  }
+  if (cp.K > 1) {  // join: the side gathers finish before anything later on s (and the temporary's free)
+    cudaEvent_t e = nullptr;
+    GBS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    evs.push_back(e);
+    GBS_CUDA_TRY(cudaEventRecord(e, side));
+    GBS_CUDA_TRY(cudaStreamWaitEvent(s, e, 0));
   }
   return GBS_OK;
 }

@@ -270,9 +270,8 @@ def csr2b2sr(A: CSR, tile: int) -> B2SR:
 
 
 def b2sr_spmm(Ab: B2SR, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-    """C = A01 @ B (FP32 out).  Hub block-rows (> 256 tiles) are summed in
-    segments that meet through float atomics (exact for integer-valued B);
-    spmm4_full_full keeps the reference's addition order everywhere."""
+    """C = A01 @ B (FP32 out).  Tile 4 reproduces spmm4_full_full_new2's
+    addition order exactly."""
     _check_cuda("B", B, tuple(_DT))
     F = int(B.shape[1])
     if out is None:
