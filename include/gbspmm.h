@@ -150,17 +150,16 @@ GBS_API gbs_status gbs_csr_spmm_cb(int nrows, int ncols, int nnz, const int *d_r
                            float *d_C, void *d_workspace, size_t workspace_bytes,
                            gbs_stream_t stream);
 
-/* Column-partitioned plan.  When B is larger than half of L2, splitting A by
- * column ranges into `parts` pieces (0 = choose: at least 2, then the
- * smallest power of two <= 8 whose B slice fits in L2; 1 when B fits in half
- * of L2 or rows of B are reused fewer than 64 times on average) and accumulating one
- * merge-path pass per piece keeps each pass's row gathers in L2 (232,965 x
- * 256 B on GB300: FP32 6.26 ms in one pass, 5.93 ms as 2 parts, 6.35 ms as
- * 4; BF16 3.71 ms -> 3.50 ms as 2 parts).  The
- * plan copies A's pattern and values into the parts (values
- * captured at creation; rebuild after changing them); with one part it only
- * records the caller's arrays, which must outlive it.  Synchronises the
- * stream.  Workspace as gbs_csr_spmm_workspace_size(nrows, nnz, F, btype). */
+/* Column-partitioned plan.  When B is larger than L2, splitting A by column
+ * ranges into `parts` pieces (0 = choose: the smallest power of two <= 8
+ * whose B slice fits in L2; 1 when B fits in L2 or rows of B are reused
+ * fewer than 64 times on average) and accumulating one merge-path pass per
+ * piece keeps each pass's row gathers in L2 (232,965 x 256 FP32 on GB300:
+ * 6.10 ms in one pass, 5.79 ms as 2 parts, 6.33 ms as 4).  The plan copies
+ * A's pattern and values into the parts (values captured at creation;
+ * rebuild after changing them); with one part it only records the caller's
+ * arrays, which must outlive it.  Synchronises the stream.  Workspace as
+ * gbs_csr_spmm_workspace_size(nrows, nnz, F, btype). */
 typedef struct gbs_csr_spmm_plan gbs_csr_spmm_plan;
 GBS_API gbs_status gbs_csr_spmm_plan_create(int nrows, int ncols, int nnz,
                                     const int *d_rowptr, const int *d_colind,

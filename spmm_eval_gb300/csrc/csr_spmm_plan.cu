@@ -1,14 +1,14 @@
 // Column-partitioned CSR SpMM plan.
 //
-// When the feature matrix B is larger than half of L2 (FP32 B of the
-// 232,965-node graph at F = 256 is 238 MB, BF16 119 MB, against 129 MB of
-// L2 split over two dies), many row gathers miss L2.  Splitting A by column
-// ranges into K parts and running the merge-path SpMM once per part with the
-// later parts accumulating into C (C += A_p B_p) keeps more of every pass's
-// gathers in L2 at the price of reading and writing C K-1 more times.
-// Measured on GB300 for that graph with the current kernels: FP32 6.26 ms in
-// one pass, 5.93 ms as 2 parts, 6.35 ms as 4; BF16 3.71 ms in one pass,
-// 3.50 ms as 2 parts (auto_parts_forward picks 2 for both).
+// When the feature matrix B is larger than L2 (FP32 B of the 232,965-node
+// graph at F = 256 is 238 MB against 129 MB of L2 split over two dies), many
+// row gathers miss L2.  Splitting A by column ranges into K parts and running
+// the merge-path SpMM once per part with the later parts accumulating into C
+// (C += A_p B_p) keeps more of every pass's gathers in L2 at the price of
+// reading and writing C K-1 more times.  Measured on GB300 for that graph
+// with the current kernels: FP32 6.10 ms in one pass, 5.79 ms as 2 parts,
+// 6.33 ms as 4; BF16 (B = 119 MB, inside L2) 3.31 ms in one pass, 3.34 ms as
+// 2 parts, 3.65 ms as 4.
 //
 // The plan copies A into the K parts once (rows in the same order, each
 // part's columns still ascending); it is reused for any B of the planned
@@ -111,15 +111,14 @@ void ColumnParts::release() {
 // 0.109 ms in one pass; the 114.8M-edge graph, ~492 per column, gains.)
 constexpr double kMinReuseForParts = 64.0;
 
-// Forward plans: once B is over half of L2, at least 2 parts, then the
-// smallest power of two whose slice fits in L2 (232,965 x 256 on GB300: FP32
-// 1 / 2 / 4 parts = 6.26 / 5.93 / 6.35 ms, BF16 3.71 / 3.50 / 3.80 ms).
+// Forward plans: once B is larger than L2, at least 2 parts, then the
+// smallest power of two whose slice fits in L2.
 gbs_status auto_parts_forward(double bbytes, long long nnz, int ncols, int *K) {
   DeviceInfo di;
   GBS_TRY(device_info(&di));
   const double l2 = (double)di.l2_bytes;
   int k = 1;
-  if (bbytes > 0.5 * l2 && (double)nnz >= kMinReuseForParts * ncols) {
+  if (bbytes > l2 && (double)nnz >= kMinReuseForParts * ncols) {
     k = 2;
     while (k < 8 && bbytes / k > l2) k *= 2;
   }

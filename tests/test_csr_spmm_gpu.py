@@ -288,3 +288,5 @@ def test_plan_auto_parts(cuda):
     g = G.uniform_rows(4096, 16)
     plan = ops.SpmmPlan(dev_csr(g, cuda), 32)
     assert plan.parts == 1  # B is tiny: no split
+    fl = G.flickr_like()
+    assert ops.SpmmPlan(dev_csr(fl, cuda), 256).parts == 1  # ~10 nonzeros per column: no split

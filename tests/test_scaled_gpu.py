@@ -110,8 +110,8 @@ def test_reddit_scale_planned(cuda, dtype):
     A = ops.CSR(g.rowptr, g.colind, None, g.nrows, g.ncols)
     d = ops.degree_rsqrt(A)
     B = G.normal(4, 5, (g.ncols, 256), device=cuda).to(dtype)
-    plan = ops.SpmmPlan(A, 256, dtype, rowscale=d, colscale=d)
-    assert plan.parts >= 2
+    plan = ops.SpmmPlan(A, 256, dtype, parts=2, rowscale=d, colscale=d)
+    assert plan.parts == 2
     C = plan.run(B)
     deg = (g.rowptr[1:] - g.rowptr[:-1]).cpu()
     rows = torch.cat([torch.topk(deg, 16).indices, torch.arange(0, g.nrows, 1999)]).numpy()
