@@ -120,9 +120,18 @@ __device__ __forceinline__ float bf16lo(uint32_t w) {
 __device__ __forceinline__ float bf16hi(uint32_t w) {
   return __uint_as_float(w & 0xffff0000u);
 }
+// FP16 pairs are widened on the FMA pipe as x * 1 + (-0), exact (the
+// mixed-precision fma.rn.f32.f16 of sm_100+): the conversion instruction it
+// replaces measured FP16 SpMM 4.02 against 3.38 ms (114.8M-edge graph, F =
+// 256).  BF16 keeps its shift / mask on the ALU: the same FMA form measured
+// 3.38 against 3.30 ms there.
 __device__ __forceinline__ float2 h2f2(uint32_t w) {
-  __half2 h = *reinterpret_cast<__half2 *>(&w);
-  return __half22float2(h);
+  float lo, hi;
+  asm("{\n .reg .b16 l, h, one;\n mov.b32 {l, h}, %2;\n mov.b16 one, 0x3C00;\n"
+      " fma.rn.f32.f16 %0, l, one, 0f80000000;\n fma.rn.f32.f16 %1, h, one, 0f80000000;\n}"
+      : "=f"(lo), "=f"(hi)
+      : "r"(w));
+  return make_float2(lo, hi);
 }
 
 }  // namespace gbs
