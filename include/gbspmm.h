@@ -351,9 +351,14 @@ GBS_API gbs_status gbs_b2sr_pack_aligned(int tile, int nblockrows,
 
 /* ------------------------------------------------------------------------
  * B2SR x dense (binary A):  C = A01 * B, C FP32 nrows x F (every row
- * written).  Tile 4 adds in the order of spmm4_full_full_new2
- * (spmm.cu:877-956), so its result is bitwise the reference's for any FP32
- * B; other tiles add in column order (exact for integer-valued B).
+ * written).  Order-free: a block-row whose tile walk is far longer than the
+ * mean work per warp (a power-law hub) is cut into segments whose partial
+ * sums are added into C with atomics, so such rows are exact for 0/1 and
+ * +-1 (integer-valued) B and within FP32 rounding otherwise, and may differ
+ * in the last bits from run to run.  Rows of other block-rows, and every
+ * row of a matrix of fewer than 1024 block-rows, add tile by tile; at tile 4
+ * in the order of spmm4_full_full_new2 (spmm.cu:877-956).  The reference's
+ * order for every row is gbs_spmm4_full_full below.
  * ------------------------------------------------------------------------ */
 GBS_API gbs_status gbs_b2sr_spmm(int tile, int nrows, int nblockrows,
                          const int *d_bsr_rowptr, const int *d_bsr_colind,

@@ -64,15 +64,17 @@ gbs_status lib_pool(cudaMemPool_t *out) {
   return GBS_OK;
 }
 
-gbs_status side_stream(cudaStream_t *out) {
+gbs_status side_stream(cudaStream_t *out, int which) {
   static std::mutex mu;
-  static cudaStream_t streams[64] = {};
+  static cudaStream_t streams[64][kSideStreams] = {};
   int dev = 0;
   GBS_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(GBS_ERR_UNSUPPORTED, "device ordinal >= 64");
+  if (which < 0 || which >= kSideStreams) return fail(GBS_ERR_INVALID_ARG, "side stream index");
   std::lock_guard<std::mutex> lock(mu);
-  if (!streams[dev]) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
-  *out = streams[dev];
+  cudaStream_t &st = streams[dev][which];
+  if (!st) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  *out = st;
   return GBS_OK;
 }
 

@@ -352,6 +352,12 @@ struct B2srSpmmArgs {
   int hub_min;
   const int *hubs;
   int slices;
+  // Order-free hub split: hub_info = [segments, tiles of all hubs], segs =
+  // (block-row, first tile) per segment; seg_warps = the warps the segment
+  // pass keeps resident.
+  const int *hub_info;
+  const int2 *segs;
+  long long seg_warps;
 };
 
 template <int TS>
@@ -376,8 +382,9 @@ __device__ __forceinline__ uint32_t tile_row_any(const void *val, size_t t, int 
   }
 }
 
-// One warp: block-row br, tile rows [grp * R, grp * R + R), feature chunks
-// chunk0 + [0, LPR * CH); U entries gathered per round.  The tiles are read
+// One warp: block-row br (tiles [tb0, te0) of it when tb0 >= 0), tile rows
+// [grp * R, grp * R + R), feature chunks chunk0 + [0, LPR * CH); U entries
+// gathered per round.  The tiles are read
 // G groups (of 32 / TS tiles = 32 entries) at a time; the entries of a step
 // that touch the warp's rows are compacted, in order, into a per-warp list in
 // shared memory (ballot + prefix popcount), and the gathers then run over the
@@ -385,9 +392,11 @@ __device__ __forceinline__ uint32_t tile_row_any(const void *val, size_t t, int 
 // Entries are added in group order and, inside a group, in lane order, so
 // every output element is the same sequence of FP32 additions as a
 // one-group-at-a-time walk.  `list` holds 32 * G entries (col, row bits).
-template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G>
+// ATOMIC: the sums are added into C (float atomics) instead of stored, and a
+// warp whose tiles hold none of its rows adds nothing.
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS, bool STORE_NZ, int U, int G, bool ATOMIC = false>
 __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long br, int grp, int chunk0,
-                                               int lane, int2 *list) {
+                                               int lane, int2 *list, int tb0 = -1, int te0 = -1) {
   constexpr int NSUB = 32 / LPR;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;  // tile rows per warp
   constexpr int TPG = 32 / TS;                          // tiles per 32 entries
@@ -410,7 +419,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
 #pragma unroll
       for (int q = 0; q < VEC; ++q) acc[k][c][q] = 0.f;
 
-  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = te0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
   const int j = REF_ORDER ? lane / TPG : lane % TS;
   const int l = REF_ORDER ? lane % TPG : lane / TS;
   // this lane's entry (feature row, row bits) in each of G groups
@@ -431,6 +440,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
     }
   };
   if (tb < te) load_step(tb);
+  int listed = 0;
   for (int s0 = tb; s0 < te; s0 += TPS) {
     int n = 0;
 #pragma unroll
@@ -439,6 +449,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
       if (nm[g] != 0) list[n + __popc(act & lt_mask)] = make_int2(nb[g], (int)nm[g]);
       n += __popc(act);
     }
+    listed += n;
     __syncwarp();
     if (s0 + TPS < te) load_step(s0 + TPS);  // next step's indices, in flight during the gathers
     for (int k0 = 0; k0 < n; k0 += U) {
@@ -474,6 +485,7 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
     }
     __syncwarp();  // the list is rewritten by the next step
   }
+  if (ATOMIC && listed == 0) return;
 #pragma unroll
   for (int k = 0; k < RPS; ++k) {
     const int tr = row0 + my0 + k;
@@ -485,7 +497,17 @@ __device__ __forceinline__ void b2sr_block_row(const B2srSpmmArgs &a, long long 
     for (int c = 0; c < CH; ++c) {
       const int chunk = chunk0 + c * LPR + sl;
       if (chunk >= a.nvec) continue;
-      if (STORE_NZ) {
+      if constexpr (ATOMIC) {
+        if constexpr (VEC % 4 == 0) {
+#pragma unroll
+          for (int q = 0; q < VEC; q += 4)
+            atomicAdd(reinterpret_cast<float4 *>(dst + (size_t)chunk * VEC + q),
+                      make_float4(acc[k][c][q], acc[k][c][q + 1], acc[k][c][q + 2], acc[k][c][q + 3]));
+        } else {
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) atomicAdd(dst + (size_t)chunk * VEC + q, acc[k][c][q]);
+        }
+      } else if (STORE_NZ) {
 #pragma unroll
         for (int q = 0; q < VEC; ++q)
           if (acc[k][c][q] != 0.f) dst[(size_t)chunk * VEC + q] = acc[k][c][q];
@@ -543,12 +565,88 @@ __global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hubs(B2srSpmmArgs a) {
   }
 }
 
+// Order-free hub split (gbs_b2sr_spmm).  The ordered hub pass above gives
+// one warp all of a hub's tiles for its (row, slice), so the largest hubs are
+// chains far longer than the mean work of a warp and the SMs idle behind
+// them.  A hub whose walk is longer than 1/kSegShare of the mean work per
+// resident warp (and than kSegMinTiles tiles) is cut into equal segments of
+// consecutive tiles (at most kSegMax); one warp per (segment, tile row,
+// feature slice) adds its partial sums into C, which the segment builder
+// zeroed.  The other hubs go to the ordered pass whole.  Sums of a split hub
+// are formed in an order that depends on scheduling: exact for 0/1 and +-1
+// features (integer partial sums), within FP32 rounding otherwise.
+constexpr int kSegMax = 64;
+constexpr int kSegMinTiles = 128;
+constexpr int kSegShare = 2;
+constexpr int SEG_U = 8;
+
+// (segments, tiles per segment) of a hub of T tiles; mean_work = tiles of
+// all hubs * items per hub / resident warps.
+__device__ __forceinline__ int2 hub_segments(int T, long long mean_work) {
+  const long long cut = max((long long)kSegMinTiles, mean_work / kSegShare);
+  if (T <= cut) return make_int2(1, T);
+  const int n = (int)min((long long)kSegMax, ((long long)T + cut - 1) / cut);
+  return make_int2(n, (T + n - 1) / n);
+}
+
+// One warp per hub: a hub that is cut appends its segments (block-row, first
+// tile) to segs and zeroes its rows of C (32-bit elements, F per row), any
+// other is appended to whole = [count, block-row ids ...].  info =
+// [segments, tiles of all hubs]; per = items per hub.
+__global__ void k_hub_segments(const int *__restrict__ hubs, const int *__restrict__ rowptr, int *__restrict__ info,
+                               int2 *__restrict__ segs, int *__restrict__ whole, long long per, long long warps,
+                               int ts, int nrows, int F, uint32_t *__restrict__ C) {
+  const int h = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (h >= __ldg(hubs)) return;
+  const int br = __ldg(hubs + 1 + h);
+  const int tb = __ldg(rowptr + br), te = __ldg(rowptr + br + 1);
+  const int2 sg = hub_segments(te - tb, (long long)__ldcg(info + 1) * per / warps);
+  if (sg.x == 1) {
+    if (lane == 0) whole[1 + atomicAdd(whole, 1)] = br;
+    return;
+  }
+  int base = 0;
+  if (lane == 0) base = atomicAdd(info, sg.x);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2(br, tb + i * sg.y);
+  const long long r0 = (long long)br * ts;
+  const int rows = (int)min((long long)ts, (long long)nrows - r0);
+  for (int i = lane; i < rows * F; i += 32) C[(r0 + i / F) * F + i % F] = 0u;
+}
+
+// One warp per (segment, tile row, feature slice), items grid-stride over a
+// grid of resident CTAs; partial sums added into C.
+template <int TS, int DT, int VEC>
+__global__ void __launch_bounds__(256, 2) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long per = (long long)TS * a.slices;
+  const long long items = (long long)__ldcg(a.hub_info) * per;
+  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * per / a.seg_warps;
+  __shared__ int2 lists[8][32 * 4];
+  for (long long it = gw; it < items; it += nw) {
+    const int2 sg = a.segs[it / per];
+    const int r = (int)(it % per);
+    const int te = __ldg(a.rowptr + sg.x + 1);
+    const int len = hub_segments(te - __ldg(a.rowptr + sg.x), mean_work).y;
+    b2sr_block_row<TS, DT, VEC, 32, 1, 1, false, SEG_U, 4, true>(a, sg.x, r / a.slices, (r % a.slices) * HUB_CHUNKS,
+                                                                 lane, lists[threadIdx.x >> 5], sg.y,
+                                                                 min(te, sg.y + len));
+  }
+}
+
 // hubs[0] = number of block-rows with more than hub_min tiles, hubs[1..] =
-// their ids (any order: each output element is computed whole by one warp).
-__global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs) {
+// their ids (any order); *tiles (if given) += their tiles.
+__global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs,
+                            int *__restrict__ tiles = nullptr) {
   const int br = blockIdx.x * blockDim.x + threadIdx.x;
   if (br >= mb) return;
-  if (rowptr[br + 1] - rowptr[br] > hub_min) hubs[1 + atomicAdd(hubs, 1)] = br;
+  const int t = rowptr[br + 1] - rowptr[br];
+  if (t > hub_min) {
+    hubs[1 + atomicAdd(hubs, 1)] = br;
+    if (tiles) atomicAdd(tiles, t);
+  }
 }
 
 namespace {
@@ -556,7 +654,8 @@ namespace {
 struct B2srVariant {
   const void *fn;
   int vec, lpr, ch, rows_per_warp, groups;
-  const void *hub_fn;  // hub pass (32-chunk slices), same tile size and type
+  const void *hub_fn;      // ordered hub pass (32-chunk slices), same tile size and type
+  const void *hub_seg_fn;  // segments of split hubs (full stores only)
 };
 
 template <int TS, int DT, int VEC, int LPR, int CH, bool NZ>
@@ -567,7 +666,8 @@ B2srVariant mk_b2sr() {
   constexpr int RPS = (NSUB * RPS1 > TS) ? ((TS / NSUB) > 0 ? TS / NSUB : 1) : RPS1;
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
   return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
-                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>};
+                     (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>,
+                     NZ ? nullptr : (const void *)&k_b2sr_spmm_hub_segs<TS, DT, VEC>};
 }
 
 template <int TS, int DT, int VEC, bool NZ>
@@ -600,9 +700,11 @@ bool is_aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u)
 
 // Per-call events (created and destroyed around one fork/join).
 struct Events {
-  cudaEvent_t e[2] = {nullptr, nullptr};
+  static constexpr int kMax = 3;
+  cudaEvent_t e[kMax] = {};
   int n = 0;
   gbs_status create(int k) {
+    if (k > kMax) return fail(GBS_ERR_INVALID_ARG, "too many events");
     for (n = 0; n < k; ++n) GBS_CUDA_TRY(cudaEventCreateWithFlags(&e[n], cudaEventDisableTiming));
     return GBS_OK;
   }
@@ -644,6 +746,9 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
   a.hub_min = 0;
   a.hubs = nullptr;
   a.slices = (a.nvec + HUB_CHUNKS - 1) / HUB_CHUNKS;
+  a.hub_info = nullptr;
+  a.segs = nullptr;
+  a.seg_warps = 1;
   const long long warps = (long long)mb * v.groups;
   const int blocks = (int)((warps * 32 + 255) / 256);
   if (mb < kHubMinBlockRows) {
@@ -651,35 +756,67 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
     GBS_CUDA_TRY(cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s));
     return GBS_OK;
   }
-  // Hub block-rows go to a concurrent pass on a side stream:
-  //   s: find hubs -> fork -> main pass (hubs skipped) -> join
-  //   side:                -> hub pass ---------------/
-  DevBuf hubs;
-  GBS_TRY(hubs.alloc(sizeof(int) * ((size_t)mb + 1), s));
-  GBS_CUDA_TRY(cudaMemsetAsync(hubs.p, 0, sizeof(int), s));
-  k_find_hubs<<<(mb + 255) / 256, 256, 0, s>>>(rowptr, mb, kHubTiles, hubs.as<int>());
+  // Hub block-rows go to concurrent passes on side streams:
+  //   s: find hubs [-> cut hubs] -> fork -> main pass (hubs skipped) -> join
+  //   side 0:                           -> whole hubs --------------/
+  //   side 1:                           -> [segments of cut hubs] -/
+  // buf = [segments, tiles of all hubs, hub count, hub ids ...]
+  DevBuf buf, segs, whole;
+  GBS_TRY(buf.alloc(sizeof(int) * ((size_t)mb + 3), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(buf.p, 0, 3 * sizeof(int), s));
+  int *info = buf.as<int>(), *hubs = info + 2;
+  k_find_hubs<<<(mb + 255) / 256, 256, 0, s>>>(rowptr, mb, kHubTiles, hubs, info + 1);
   GBS_TRY(check_launch("k_find_hubs"));
   a.hub_min = kHubTiles;
-  a.hubs = hubs.as<int>();
-  cudaStream_t side = nullptr;
-  GBS_TRY(side_stream(&side));
-  Events ev;
-  GBS_TRY(ev.create(2));
-  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
-  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  a.hubs = hubs;
   DeviceInfo di;
   GBS_TRY(device_info(&di));
+  B2srSpmmArgs aw = a;  // the ordered pass: all hubs, or those not cut
+  dim3 seg_grid;
+  if (v.hub_seg_fn) {
+    int per_sm = 0;
+    GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.hub_seg_fn, 256, 0));
+    seg_grid = dim3(di.sm_count * (per_sm > 0 ? per_sm : 1));
+    GBS_TRY(segs.alloc(sizeof(int2) * (size_t)mb * kSegMax, s));
+    GBS_TRY(whole.alloc(sizeof(int) * ((size_t)mb + 1), s));
+    GBS_CUDA_TRY(cudaMemsetAsync(whole.p, 0, sizeof(int), s));
+    a.hub_info = info;
+    a.segs = segs.as<int2>();
+    a.seg_warps = (long long)seg_grid.x * 8;
+    k_hub_segments<<<(mb + 7) / 8, 256, 0, s>>>(hubs, rowptr, info, segs.as<int2>(), whole.as<int>(),
+                                                (long long)ts * a.slices, a.seg_warps, ts, nrows, F,
+                                                reinterpret_cast<uint32_t *>(C));
+    GBS_TRY(check_launch("k_hub_segments"));
+    aw.hubs = whole.as<int>();
+  }
+  cudaStream_t side = nullptr, side1 = nullptr;
+  GBS_TRY(side_stream(&side, 0));
+  if (v.hub_seg_fn) GBS_TRY(side_stream(&side1, 1));
+  Events ev;
+  GBS_TRY(ev.create(3));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  if (side1) GBS_CUDA_TRY(cudaStreamWaitEvent(side1, ev.e[0], 0));
   void *args[] = {&a};
+  void *wargs[] = {&aw};
+  gbs_status st = GBS_OK;
+  cudaError_t e = cudaSuccess;
+  if (side1) {
+    e = cudaLaunchKernel(v.hub_seg_fn, seg_grid, dim3(256), args, 0, side1);
+    if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_spmm_hub_segs");
+    GBS_CUDA_TRY(cudaEventRecord(ev.e[2], side1));
+  }
   // enough warps that every (hub, group, slice) item of a typical graph gets
   // its own warp (surplus warps exit at once)
-  GBS_CUDA_TRY(cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), args, 0, side));
+  e = cudaLaunchKernel(v.hub_fn, dim3(di.sm_count * 8), dim3(256), wargs, 0, side);
+  if (e != cudaSuccess && st == GBS_OK) st = cuda_fail(e, "k_b2sr_spmm_hubs");
   GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
-  gbs_status st = GBS_OK;
-  cudaError_t e = cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s);
-  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_spmm");
-  // join even on failure, so the side stream's work is ordered before
-  // anything the caller enqueues next (and before the list is freed)
+  e = cudaLaunchKernel(v.fn, dim3(blocks), dim3(256), args, 0, s);
+  if (e != cudaSuccess && st == GBS_OK) st = cuda_fail(e, "k_b2sr_spmm");
+  // join even on failure, so the side streams' work is ordered before
+  // anything the caller enqueues next (and before the lists are freed)
   GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[1], 0));
+  if (side1) GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[2], 0));
   return st;
 }
 
@@ -701,6 +838,10 @@ struct B2srBmmArgs {
   int signed_form;
   int hub_min;      // main pass: leave block-rows of more tiles to the hub pass (0: none)
   const int *hubs;  // hub pass: [count, block-row ids ...]
+  // hub split, as in B2srSpmmArgs
+  const int *hub_info;
+  const int2 *segs;
+  long long seg_warps;
 };
 
 // One warp: block-row br, tile rows [grp * R, grp * R + R).  Entries of G
@@ -820,9 +961,12 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
 // (entry, word) -- 32 / WMAX entries per warp-wide load, so a round needs
 // WMAX loads per lane and no more registers -- and each word is broadcast to
 // the lanes by a shuffle when its bits are counted.  The chain of dependent
-// round trips is (entries / 32) deep instead of (entries / U).
-template <int TS, int WMAX, bool AL>
-__device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list) {
+// round trips is (entries / 32) deep instead of (entries / U).  With
+// tb0 >= 0 only tiles [tb0, te0) are walked; ATOMIC adds the counts (and the
+// +-1 form's 2 * count - entries, which is additive) into C.
+template <int TS, int WMAX, bool AL, bool ATOMIC = false>
+__device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list,
+                                            int tb0 = -1, int te0 = -1) {
   constexpr int G = 4;
   constexpr int TPG = 32 / TS;
   constexpr int TPS = TPG * G;
@@ -832,7 +976,7 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
   int deg = 0;
 #pragma unroll
   for (int k = 0; k < WMAX; ++k) cnt[k] = 0;
-  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = tb0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
   const int j = lane % TS, l = lane / TS;
   const int shift = 31 - lane;
   const int my_e = lane / WMAX, my_w = lane % WMAX;  // (entry, word) this lane loads
@@ -874,12 +1018,16 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
     __syncwarp();
   }
   const long long orow = br * TS + row;
-  if (orow >= a.nrows) return;
+  if (orow >= a.nrows || (ATOMIC && deg == 0)) return;
   int32_t *dst = a.C + (size_t)orow * a.F;
 #pragma unroll
   for (int k = 0; k < WMAX; ++k) {
     const int c = k * 32 + lane;
-    if (c < a.F) dst[c] = a.signed_form ? 2 * cnt[k] - deg : cnt[k];
+    const int v = a.signed_form ? 2 * cnt[k] - deg : cnt[k];
+    if (c < a.F) {
+      if constexpr (ATOMIC) atomicAdd(dst + c, v);
+      else dst[c] = v;
+    }
   }
 }
 
@@ -897,15 +1045,35 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
   }
 }
 
+// Segments of cut hubs (k_hub_segments): one warp per (segment, tile row),
+// counts added into C.
+template <int TS, int WMAX, bool AL>
+__global__ void __launch_bounds__(256) k_b2sr_bmm_hub_segs(B2srBmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long items = (long long)__ldcg(a.hub_info) * TS;
+  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * TS / a.seg_warps;
+  __shared__ int2 lists[8][32 * 4];
+  for (long long it = gw; it < items; it += nw) {
+    const int2 sg = a.segs[it / TS];
+    const int te = __ldg(a.rowptr + sg.x + 1);
+    const int len = hub_segments(te - __ldg(a.rowptr + sg.x), mean_work).y;
+    bmm_hub_row<TS, WMAX, AL, true>(a, sg.x, (int)(it % TS), lane, lists[threadIdx.x >> 5], sg.y,
+                                    min(te, sg.y + len));
+  }
+}
+
 template <int TS, bool AL = false>
 gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
-  const void *fn = nullptr, *hub_fn = nullptr;
+  const void *fn = nullptr, *hub_fn = nullptr, *seg_fn = nullptr;
   int wmax = 0;
-#define GBS_BMM_CASE(WM)                                 \
-  {                                                      \
-    fn = (const void *)&k_b2sr_bmm<TS, WM, AL>;          \
-    hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM, AL>; \
-    wmax = WM;                                           \
+#define GBS_BMM_CASE(WM)                                     \
+  {                                                          \
+    fn = (const void *)&k_b2sr_bmm<TS, WM, AL>;              \
+    hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM, AL>;     \
+    seg_fn = (const void *)&k_b2sr_bmm_hub_segs<TS, WM, AL>; \
+    wmax = WM;                                               \
   }
   if (a.W <= 1) GBS_BMM_CASE(1)
   else if (a.W <= 2) GBS_BMM_CASE(2)
@@ -923,34 +1091,61 @@ gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   if (blocks == 0) return GBS_OK;
   a.hub_min = 0;
   a.hubs = nullptr;
+  a.hub_info = nullptr;
+  a.segs = nullptr;
+  a.seg_warps = 1;
   if (a.mb < kHubMinBlockRows) {
     void *args[] = {&a};
     GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s));
     return GBS_OK;
   }
-  // main pass on s, hub pass on the side stream (as in b2sr_spmm_run)
-  DevBuf hubs;
-  GBS_TRY(hubs.alloc(sizeof(int) * ((size_t)a.mb + 1), s));
-  GBS_CUDA_TRY(cudaMemsetAsync(hubs.p, 0, sizeof(int), s));
-  k_find_hubs<<<(a.mb + 255) / 256, 256, 0, s>>>(a.rowptr, a.mb, kHubTiles, hubs.as<int>());
+  // main pass on s, whole hubs and segments of cut hubs on the side streams
+  // (as in b2sr_spmm_run; integer counts, so the split is exact)
+  DevBuf buf, segs, whole;
+  GBS_TRY(buf.alloc(sizeof(int) * ((size_t)a.mb + 3), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(buf.p, 0, 3 * sizeof(int), s));
+  int *info = buf.as<int>(), *hubs = info + 2;
+  k_find_hubs<<<(a.mb + 255) / 256, 256, 0, s>>>(a.rowptr, a.mb, kHubTiles, hubs, info + 1);
   GBS_TRY(check_launch("k_find_hubs"));
   a.hub_min = kHubTiles;
-  a.hubs = hubs.as<int>();
-  cudaStream_t side = nullptr;
-  GBS_TRY(side_stream(&side));
-  Events ev;
-  GBS_TRY(ev.create(2));
-  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
-  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  a.hubs = hubs;
   DeviceInfo di;
   GBS_TRY(device_info(&di));
+  int per_sm = 0;
+  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, seg_fn, 256, 0));
+  const dim3 seg_grid(di.sm_count * (per_sm > 0 ? per_sm : 1));
+  GBS_TRY(segs.alloc(sizeof(int2) * (size_t)a.mb * kSegMax, s));
+  GBS_TRY(whole.alloc(sizeof(int) * ((size_t)a.mb + 1), s));
+  GBS_CUDA_TRY(cudaMemsetAsync(whole.p, 0, sizeof(int), s));
+  a.hub_info = info;
+  a.segs = segs.as<int2>();
+  a.seg_warps = (long long)seg_grid.x * 8;
+  k_hub_segments<<<(a.mb + 7) / 8, 256, 0, s>>>(hubs, a.rowptr, info, segs.as<int2>(), whole.as<int>(), TS,
+                                                a.seg_warps, TS, a.nrows, a.F, reinterpret_cast<uint32_t *>(a.C));
+  GBS_TRY(check_launch("k_hub_segments"));
+  B2srBmmArgs aw = a;
+  aw.hubs = whole.as<int>();
+  cudaStream_t side = nullptr, side1 = nullptr;
+  GBS_TRY(side_stream(&side, 0));
+  GBS_TRY(side_stream(&side1, 1));
+  Events ev;
+  GBS_TRY(ev.create(3));
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[0], s));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(side1, ev.e[0], 0));
   void *args[] = {&a};
-  GBS_CUDA_TRY(cudaLaunchKernel(hub_fn, dim3(di.sm_count * 4), dim3(256), args, 0, side));
-  GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
+  void *wargs[] = {&aw};
   gbs_status st = GBS_OK;
-  cudaError_t e = cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s);
-  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_bmm");
+  cudaError_t e = cudaLaunchKernel(seg_fn, seg_grid, dim3(256), args, 0, side1);
+  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_bmm_hub_segs");
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[2], side1));
+  e = cudaLaunchKernel(hub_fn, dim3(di.sm_count * 4), dim3(256), wargs, 0, side);
+  if (e != cudaSuccess && st == GBS_OK) st = cuda_fail(e, "k_b2sr_bmm_hubs");
+  GBS_CUDA_TRY(cudaEventRecord(ev.e[1], side));
+  e = cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s);
+  if (e != cudaSuccess && st == GBS_OK) st = cuda_fail(e, "k_b2sr_bmm");
   GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[1], 0));
+  GBS_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[2], 0));
   return st;
 }
 

@@ -24,9 +24,11 @@ inline int bits_for(long long v) {
 // synchronisation).  gbs_pool_trim releases what it keeps.
 constexpr unsigned long long kPoolKeepBytes = 8ull << 30;
 gbs_status lib_pool(cudaMemPool_t *out);
-// A non-blocking stream per device for a sub-pass that runs beside the
-// caller's stream (forked and joined with events inside one call).
-gbs_status side_stream(cudaStream_t *out);
+// Non-blocking streams per device (kSideStreams of them, by index) for
+// sub-passes that run beside the caller's stream (forked and joined with
+// events inside one call).
+constexpr int kSideStreams = 2;
+gbs_status side_stream(cudaStream_t *out, int which = 0);
 
 // RAII device buffer from stream-ordered allocation in the library pool
 // (freed on the same stream).  Used only where an entry point documents that

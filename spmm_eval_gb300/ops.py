@@ -270,8 +270,10 @@ def csr2b2sr(A: CSR, tile: int) -> B2SR:
 
 
 def b2sr_spmm(Ab: B2SR, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-    """C = A01 @ B (FP32 out).  Tile 4 reproduces spmm4_full_full_new2's
-    addition order exactly."""
+    """C = A01 @ B (FP32 out).  Hub block-rows are split and summed with
+    atomics (order-free: exact on 0/1 and +-1 features, FP32 rounding
+    otherwise); ``spmm4_full_full`` keeps spmm4_full_full_new2's addition
+    order for every row."""
     _check_cuda("B", B, tuple(_DT))
     F = int(B.shape[1])
     if out is None:

@@ -7,9 +7,9 @@ their file:line) and loaded through the driver API (``oracle/refkern.py``),
 each launched with the grid the reference uses.  Checked bit for bit:
 
 * ``spmm4_full_full_new2`` (backend/spmm.cu:877-956, launched as
-  test_spmm_full.cu:351-361) against ``gbs_spmm4_full_full`` and
-  ``gbs_b2sr_spmm`` tile 4 on arbitrary FP32 features, and against the
-  oracle's restatement of its addition order;
+  test_spmm_full.cu:351-361) against ``gbs_spmm4_full_full`` on arbitrary
+  FP32 features (and ``gbs_b2sr_spmm`` tile 4 where it splits no hub), and
+  against the oracle's restatement of its addition order;
 * ``ToBit{4,8,16,32}Col<float>`` applied to cuSPARSE csr2bsr blocks (the
   chain inside csr2bsr_batch_{4,8,16,32}, csr2bsr_batch_bsrbmv.cu:296-339)
   against the library's packer;
@@ -73,7 +73,11 @@ def test_fbf_bitwise_vs_reference_kernel(cuda, rk, gi, F):
     torch.cuda.synchronize()
     assert torch.equal(mine.view(torch.int32), ref.view(torch.int32))
     full = ops.b2sr_spmm(Ab, Bd)
-    assert torch.equal(full.view(torch.int32), ref[:n].view(torch.int32))
+    if Ab.nblockrows < 1024:  # one pass, no hub split: the reference's order
+        assert torch.equal(full.view(torch.int32), ref[:n].view(torch.int32))
+    else:  # split hubs summed with atomics: FP32 rounding against FP64
+        r64, mag = oracle.csr_spmm_f64(rp, ci, None, B)
+        assert oracle.rel_err(full.cpu().numpy(), r64, mag)[0] <= 1e-5
     if m * F <= 4_000_000:  # the oracle's restatement of the order, pinned
         brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, 4)
         want = oracle.b2sr4_spmm_ref(n, brp, bci, bv, B)
