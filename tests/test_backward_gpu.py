@@ -249,6 +249,41 @@ def test_planned_backward_widths(cuda, dtype, F):
     assert np.max(np.abs(dv.cpu().numpy() - refv) / np.maximum(S, 1e-30)) <= 1e-5
 
 
+@pytest.mark.parametrize("dtype, K", [(torch.float32, 4), (torch.bfloat16, 2)])
+def test_planned_backward_auto_reddit(cuda, dtype, K):
+    """The 232,965-node graph at F = 256 through the automatic split (the
+    fewest equal row ranges of A whose dC slice fits in half of L2: 4 for
+    FP32 dC, 2 for BF16): dB on sampled rows of A^T (incl. the 16 largest)
+    and dvals on the entries of sampled rows of A against FP64, and both
+    against the plan with one more range."""
+    g = G.gcn_normalize(G.reddit_like(device=cuda))
+    n, F = g.nrows, 256
+    T = ops.CSRTranspose(ops.CSR(g.rowptr, g.colind, None, n, n))
+    tv = T.values(g.vals)
+    Gd = G.normal(4, 51, (n, F), device=cuda).to(dtype)
+    Hd = G.normal(4, 52, (n, F), device=cuda).to(dtype)
+    plan = ops.BackwardPlan(T, tv, F, dtype, 0)
+    assert plan.parts == K
+    dB, dv = plan.run(Gd, Hd)
+    dBe, dve = ops.BackwardPlan(T, tv, F, dtype, K + 1).run(Gd, Hd)
+    assert torch.allclose(dB, dBe, rtol=1e-5, atol=1e-6)
+    assert torch.allclose(dv, dve, rtol=1e-6, atol=1e-7)
+    Gr, Hr = Gd.float().cpu().numpy(), Hd.float().cpu().numpy()
+    trp, tci, _ = (x.cpu().numpy() for x in T.arrays())
+    tdeg = torch.from_numpy(np.diff(trp))
+    rows = torch.cat([torch.topk(tdeg, 16).indices, torch.arange(0, n, 1999)]).numpy()
+    ref, mag = oracle.csr_spmm_f64(trp, tci, tv.cpu().numpy(), Gr, rows=rows)
+    assert oracle.rel_err(dB.cpu().numpy()[rows], ref, mag)[0] <= 1e-5
+    rp, ci = g.rowptr.cpu().numpy(), g.colind.cpu().numpy()
+    sel = np.arange(7, n, 2999)
+    cnt = rp[sel + 1] - rp[sel]
+    srp = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
+    idx = np.concatenate([np.arange(rp[r], rp[r + 1]) for r in sel])
+    refv = oracle.sddmm_f64(srp, ci[idx], Gr[sel], Hr)
+    S = sddmm_scale(srp, ci[idx], Gr[sel], Hr)
+    assert np.max(np.abs(dv.cpu().numpy()[idx] - refv) / np.maximum(S, 1e-30)) <= 1e-5
+
+
 def test_planned_backward_auto_parts_and_reuse(cuda):
     """Automatic part count (1 when dC fits in half of L2) and a plan reused
     across calls with a shared workspace."""
