@@ -636,6 +636,227 @@ __global__ void __launch_bounds__(256, 2) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tile-wide B2SR SpMM (gbs_b2sr_spmm, tiles 8 / 16 / 32).  The kernels above
+// give a warp R rows of a block-row, so at large tiles every tile is walked
+// TS / R times (and TS times in the hub pass): at tile 32 the walk of the
+// tile indices and row words, not the gathers, is the work.  Here one warp
+// owns all TS rows of a block-row and a slice of 128 features (4 per lane),
+// with the row sums in shared memory, and reads each tile once: per step
+// the indices of 32 tiles (one per lane) and their row words (lane = tile
+// row, 32 / TS tiles per load, all TS loads issued together), whose set
+// bits are appended to a per-warp
+// list of (tile, row, column) entries; the list is then gathered U at a
+// time, every gathered 4-feature chunk added to its row's sums.  Entries of
+// a row come in column order, as in the kernels above, so a row's sums are
+// the same sequence of FP32 additions.  Block-rows longer than half the mean
+// work per resident warp are cut into segments (k_wide_segments) whose sums
+// are added into C with atomics, as the hub split above.
+constexpr int WIDE_WARPS = 4;    // warps per CTA
+constexpr int WIDE_FEATS = 128;  // features per item: 4 per lane
+constexpr int WIDE_U = 8;        // gathers in flight per lane
+constexpr int kWideCutMin = 256; // tiles: shorter block-rows are never cut
+
+template <int TS>
+constexpr int wide_cap() { return 32 * TS; }  // list entries: the bits of 32 / TS tiles at most
+template <int TS>
+constexpr size_t wide_smem() {
+  return (size_t)WIDE_WARPS * (TS * 32 * sizeof(float4) + wide_cap<TS>() * sizeof(uint16_t));
+}
+
+// Block-rows of more tiles than this are cut: half the mean work per
+// resident warp, in tiles (nnzb tiles x slices items / warps).
+__device__ __forceinline__ long long wide_cut(long long nnzb, int slices, long long warps) {
+  return max((long long)kWideCutMin, nnzb * slices / (2 * warps));
+}
+// (segments, tiles per segment) of a cut block-row of T tiles.
+__device__ __forceinline__ int2 wide_segments(int T, long long cut) {
+  const int n = (int)min((long long)kSegMax, ((long long)T + cut - 1) / cut);
+  return make_int2(n, (T + n - 1) / n);
+}
+
+// One warp per block-row: a block-row longer than the cut appends its
+// segments (block-row, first tile) to segs, counted in *nsegs, and zeroes its
+// rows of C (F features, ldc = F).
+template <int TS>
+__global__ void k_wide_segments(B2srSpmmArgs a, int *__restrict__ nsegs, int2 *__restrict__ segs) {
+  const long long br = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (br >= a.mb) return;
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const long long cut = wide_cut(__ldg(a.rowptr + a.mb), a.slices, a.seg_warps);
+  if (te - tb <= cut) return;
+  const int2 sg = wide_segments(te - tb, cut);
+  int base = 0;
+  if (lane == 0) base = atomicAdd(nsegs, sg.x);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2((int)br, tb + i * sg.y);
+  const long long r0 = br * TS;
+  const int rows = (int)min((long long)TS, (long long)a.nrows - r0);
+  const int F = (int)a.ldc;
+  for (int i = lane; i < rows * F; i += 32) a.C[(r0 + i / F) * a.ldc + i % F] = 0.f;
+}
+
+// 4 features of a B row as FP32 (16-byte FP32 or 8-byte 16-bit load).
+template <int DT>
+__device__ __forceinline__ float4 wide_load(const void *B, size_t elem) {
+  if constexpr (DT == DT_F32) {
+    return ld_nc_f4(reinterpret_cast<const float *>(B) + elem);
+  } else {
+    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const uint16_t *>(B) + elem));
+    if constexpr (DT == DT_BF16) {
+      return make_float4(bf16lo(w.x), bf16hi(w.x), bf16lo(w.y), bf16hi(w.y));
+    } else {
+      const float2 p = h2f2(w.x), q = h2f2(w.y);
+      return make_float4(p.x, p.y, q.x, q.y);
+    }
+  }
+}
+
+// Gathers of the n listed entries, WIDE_U at a time, each 4-feature chunk
+// added to its row's sums (entry = tile << 10 | row << 5 | column; the
+// tile's block column is lane `tile`'s tc).
+template <int TS, int DT>
+__device__ __forceinline__ void wide_flush(const B2srSpmmArgs &a, const uint16_t *list, int n, int tc_lane,
+                                           int f0, bool mine, int lane, float4 *acc) {
+  __syncwarp();
+  for (int k0 = 0; k0 < n; k0 += WIDE_U) {
+    float4 x[WIDE_U];
+    int rr[WIDE_U];
+#pragma unroll
+    for (int u = 0; u < WIDE_U; ++u) {
+      const bool live = k0 + u < n;
+      const int e = live ? (int)list[k0 + u] : 0;
+      rr[u] = (e >> 5) & 31;
+      const int tc = __shfl_sync(0xffffffffu, tc_lane, e >> 10);
+      const size_t col = (size_t)(unsigned)tc * TS + (e & 31);
+      x[u] = (live && mine) ? wide_load<DT>(a.B, col * (size_t)a.ldb + f0) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < WIDE_U; ++u) {
+      if (k0 + u < n) {
+        float4 t = acc[rr[u] * 32 + lane];
+        t.x = t.x + x[u].x;
+        t.y = t.y + x[u].y;
+        t.z = t.z + x[u].z;
+        t.w = t.w + x[u].w;
+        acc[rr[u] * 32 + lane] = t;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// The same, out of line: the flush of a full list inside the unrolled group
+// loop (rare: a step of more than 32 * TS bits), kept out of the loop body
+// so that the loop's code stays small.
+template <int TS, int DT>
+__device__ __noinline__ void wide_flush_full(const B2srSpmmArgs &a, const uint16_t *list, int n, int tc_lane,
+                                             int f0, bool mine, int lane, float4 *acc) {
+  wide_flush<TS, DT>(a, list, n, tc_lane, f0, mine, lane, acc);
+}
+
+// One warp: tiles [tb, te) of block-row br, features [sl * 128, +128).
+template <int TS, int DT>
+__device__ __forceinline__ void wide_block_row(const B2srSpmmArgs &a, long long br, int tb, int te, int sl,
+                                               bool atomic, int lane, float4 *acc, uint16_t *list) {
+  constexpr int CAP = wide_cap<TS>();
+  constexpr int TPG = 32 / TS;
+  const int F = (int)a.ldc;
+  const int f0 = sl * WIDE_FEATS + lane * 4;
+  const bool mine = f0 < F;  // F % 4 == 0: all 4 features in range
+#pragma unroll
+  for (int r = 0; r < TS; ++r) acc[r * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int s0 = tb; s0 < te; s0 += 32) {
+    const int nt = min(32, te - s0);
+    // the step's tile indices and row words, all loads in flight together:
+    // group g holds tiles g * TPG + [0, TPG), lane = (tile - g * TPG) * TS + row
+    const int my_tc = lane < nt ? __ldg(a.colind + s0 + lane) : 0;
+    uint32_t wv[TS];
+#pragma unroll
+    for (int g = 0; g < TS; ++g) {
+      const int i = g * TPG + lane / TS;
+      wv[g] = i < nt ? tile_row<TS>(a.val, (size_t)(s0 + i), lane % TS) : 0u;
+    }
+    int n = 0;
+#pragma unroll
+    for (int g = 0; g < TS; ++g) {
+      if (g * TPG >= nt) break;
+      uint32_t w = wv[g];
+      const unsigned nzm = __ballot_sync(0xffffffffu, w != 0);
+      if (nzm == 0) continue;
+      const int cnt = __popc(w);
+      int tot, excl;
+      if (__ballot_sync(0xffffffffu, cnt > 1) == 0) {  // at most one bit per lane
+        tot = __popc(nzm);
+        excl = __popc(nzm & lt_mask);
+      } else {
+        tot = __reduce_add_sync(0xffffffffu, cnt);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        excl = incl - cnt;
+      }
+      if (n + tot > CAP) {  // warp-uniform; one group's bits always fit in an empty list
+        wide_flush_full<TS, DT>(a, list, n, my_tc, f0, mine, lane, acc);
+        n = 0;
+      }
+      int pos = n + excl;
+      const int i = g * TPG + lane / TS, r = lane % TS;
+      while (w) {  // column 0 is the most significant of the TS bits: ascending columns
+        const int b = 31 - __clz(w);
+        list[pos++] = (uint16_t)((i << 10) | (r << 5) | (TS - 1 - b));
+        w &= ~(1u << b);
+      }
+      n += tot;
+    }
+    wide_flush<TS, DT>(a, list, n, my_tc, f0, mine, lane, acc);
+  }
+  if (!mine) return;
+  for (int r = 0; r < TS; ++r) {
+    const long long orow = br * TS + r;
+    if (orow >= a.nrows) break;
+    const float4 v = acc[r * 32 + lane];
+    float *dst = a.C + (size_t)orow * a.ldc + f0;
+    if (atomic) atomicAdd(reinterpret_cast<float4 *>(dst), v);
+    else *reinterpret_cast<float4 *>(dst) = v;
+  }
+}
+
+// Items: (block-row, slice) for every block-row not cut, then (segment,
+// slice) for the segments of the cut ones; grid-stride over resident CTAs.
+template <int TS, int DT>
+__global__ void __launch_bounds__(WIDE_WARPS * 32, 1) k_b2sr_spmm_wide(B2srSpmmArgs a) {
+  extern __shared__ __align__(16) unsigned char wide_sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float4 *acc = reinterpret_cast<float4 *>(wide_sm) + (size_t)warp * TS * 32;
+  uint16_t *list = reinterpret_cast<uint16_t *>(wide_sm + (size_t)WIDE_WARPS * TS * 32 * sizeof(float4)) +
+                   (size_t)warp * wide_cap<TS>();
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long cut = wide_cut(__ldg(a.rowptr + a.mb), a.slices, a.seg_warps);
+  const long long main_items = (long long)a.mb * a.slices;
+  const long long items = main_items + (long long)__ldcg(a.hub_info) * a.slices;
+  for (long long it = gw; it < items; it += nw) {
+    const int sl = (int)(it % a.slices);
+    if (it < main_items) {
+      const long long br = it / a.slices;
+      const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+      if (te - tb > cut) continue;  // done by its segments
+      wide_block_row<TS, DT>(a, br, tb, te, sl, false, lane, acc, list);
+    } else {
+      const int2 sg = a.segs[(it - main_items) / a.slices];
+      const int te = __ldg(a.rowptr + sg.x + 1);
+      const int len = wide_segments(te - __ldg(a.rowptr + sg.x), cut).y;
+      wide_block_row<TS, DT>(a, sg.x, sg.y, min(te, sg.y + len), sl, true, lane, acc, list);
+    }
+  }
+}
+
 // hubs[0] = number of block-rows with more than hub_min tiles, hubs[1..] =
 // their ids (any order); *tiles (if given) += their tiles.
 __global__ void k_find_hubs(const int *__restrict__ rowptr, int mb, int hub_min, int *__restrict__ hubs,
@@ -713,6 +934,57 @@ struct Events {
   }
 };
 
+template <int TS, int DT>
+gbs_status launch_wide(B2srSpmmArgs &a, cudaStream_t s) {
+  const void *fn = (const void *)&k_b2sr_spmm_wide<TS, DT>;
+  const size_t smem = wide_smem<TS>();
+  GBS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  int per_sm = 0;
+  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WIDE_WARPS * 32, smem));
+  const dim3 grid(di.sm_count * (per_sm > 0 ? per_sm : 1));
+  a.seg_warps = (long long)grid.x * WIDE_WARPS;
+  DevBuf info, segs;
+  GBS_TRY(info.alloc(sizeof(int), s));
+  GBS_TRY(segs.alloc(sizeof(int2) * (size_t)a.mb * kSegMax, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(info.p, 0, sizeof(int), s));
+  k_wide_segments<TS><<<(int)(((long long)a.mb * 32 + 255) / 256), 256, 0, s>>>(a, info.as<int>(), segs.as<int2>());
+  GBS_TRY(check_launch("k_wide_segments"));
+  a.hub_info = info.as<int>();
+  a.segs = segs.as<int2>();
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(WIDE_WARPS * 32), args, smem, s));
+  return GBS_OK;
+}
+
+gbs_status b2sr_spmm_wide(int ts, int nrows, int mb, const int *rowptr, const int *colind, const void *val,
+                          const void *B, int dt, int F, float *C, cudaStream_t s) {
+  B2srSpmmArgs a{};
+  a.nrows = nrows;
+  a.mb = mb;
+  a.rowptr = rowptr;
+  a.colind = colind;
+  a.val = val;
+  a.B = B;
+  a.nvec = F / 4;
+  a.ldb = F;
+  a.ldc = F;
+  a.C = C;
+  a.slices = (F + WIDE_FEATS - 1) / WIDE_FEATS;
+#define GBS_WIDE(TS)                                           \
+  if (ts == TS) {                                               \
+    if (dt == DT_F32) return launch_wide<TS, DT_F32>(a, s);    \
+    if (dt == DT_BF16) return launch_wide<TS, DT_BF16>(a, s);  \
+    return launch_wide<TS, DT_F16>(a, s);                      \
+  }
+  GBS_WIDE(8)
+  GBS_WIDE(16)
+  GBS_WIDE(32)
+#undef GBS_WIDE
+  return fail(GBS_ERR_UNSUPPORTED, "b2sr spmm: the tile-wide pass takes tiles 8, 16 and 32");
+}
+
 }  // namespace
 
 gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *rowptr, const int *colind,
@@ -732,6 +1004,13 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
                 "b2sr spmm: F too large (FP32 <= 1024 with 16-byte alignment, else <= 256; 16-bit "
                 "features need F % 8 == 0, F <= 2048)");
   if (mb == 0) return GBS_OK;
+  // tiles 16 / 32 of the full-output entry point: the tile-wide pass (4
+  // features per lane: FP32 16-byte or 16-bit 8-byte aligned B, F % 4 ==
+  // 0).  At tile 8 the row-group kernels above are faster (flickr-shaped
+  // graph, F = 256: 0.33 against 0.46 ms).
+  if (!store_nz && ts >= 16 && F % 4 == 0 && is_aligned16(C) &&
+      (dt == DT_F32 ? is_aligned16(B) : (reinterpret_cast<uintptr_t>(B) & 7u) == 0))
+    return b2sr_spmm_wide(ts, nrows, mb, rowptr, colind, val, B, dt, F, C, s);
   B2srSpmmArgs a;
   a.nrows = nrows;
   a.mb = mb;
