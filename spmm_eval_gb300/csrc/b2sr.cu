@@ -643,9 +643,8 @@ __global__ void __launch_bounds__(256, 2) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
 // tile indices and row words, not the gathers, is the work.  Here one warp
 // owns all TS rows of a block-row and a slice of 128 features (4 per lane),
 // with the row sums in shared memory, and reads each tile once: per step
-// the indices of 32 tiles (one per lane) and their row words (lane = tile
-// row, 32 / TS tiles per load, all TS loads issued together), whose set
-// bits are appended to a per-warp
+// the indices of 32 tiles (one per lane) and their row words (TS per lane,
+// all issued together), whose set bits are appended to a per-warp
 // list of (tile, row, column) entries; the list is then gathered U at a
 // time, every gathered 4-feature chunk added to its row's sums.  Entries of
 // a row come in column order, as in the kernels above, so a row's sums are
@@ -747,80 +746,92 @@ __device__ __forceinline__ void wide_flush(const B2srSpmmArgs &a, const uint16_t
   __syncwarp();
 }
 
-// The same, out of line: the flush of a full list inside the unrolled group
-// loop (rare: a step of more than 32 * TS bits), kept out of the loop body
-// so that the loop's code stays small.
+// A step whose bits overflow the list (more than 32 * TS of them), out of
+// line: its tiles one at a time (lane = tile row), flushing whenever the
+// next tile might not fit.  Rows still add in tile and column order.
 template <int TS, int DT>
-__device__ __noinline__ void wide_flush_full(const B2srSpmmArgs &a, const uint16_t *list, int n, int tc_lane,
-                                             int f0, bool mine, int lane, float4 *acc) {
+__device__ __noinline__ void wide_step_dense(const B2srSpmmArgs &a, int s0, int nt, int tc_lane, int f0, bool mine,
+                                             int lane, float4 *acc, uint16_t *list) {
+  constexpr int CAP = wide_cap<TS>();
+  int n = 0;
+  for (int i = 0; i < nt; ++i) {
+    uint32_t w = lane < TS ? tile_row<TS>(a.val, (size_t)(s0 + i), lane) : 0u;
+    const int cnt = __popc(w);
+    const int tot = __reduce_add_sync(0xffffffffu, cnt);
+    if (n + tot > CAP) {  // one tile (TS * TS bits) always fits in an empty list
+      wide_flush<TS, DT>(a, list, n, tc_lane, f0, mine, lane, acc);
+      n = 0;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int pos = n + incl - cnt;
+    while (w) {
+      const int b = 31 - __clz(w);
+      list[pos++] = (uint16_t)((i << 10) | (lane << 5) | (TS - 1 - b));
+      w &= ~(1u << b);
+    }
+    n += tot;
+  }
   wide_flush<TS, DT>(a, list, n, tc_lane, f0, mine, lane, acc);
 }
 
 // One warp: tiles [tb, te) of block-row br, features [sl * 128, +128).
+// Per step of 32 tiles, lane (k, r) = (lane / TS, lane % TS) loads row r of
+// tiles k * TS + [0, TS) and appends its set bits (tiles ascending, columns
+// ascending) at its place in the list (one prefix sum per step), so every
+// row's entries are in the list in tile and column order.
 template <int TS, int DT>
 __device__ __forceinline__ void wide_block_row(const B2srSpmmArgs &a, long long br, int tb, int te, int sl,
                                                bool atomic, int lane, float4 *acc, uint16_t *list) {
   constexpr int CAP = wide_cap<TS>();
-  constexpr int TPG = 32 / TS;
   const int F = (int)a.ldc;
   const int f0 = sl * WIDE_FEATS + lane * 4;
   const bool mine = f0 < F;  // F % 4 == 0: all 4 features in range
+  const int k0 = (lane / TS) * TS, r = lane % TS;
 #pragma unroll
-  for (int r = 0; r < TS; ++r) acc[r * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int q = 0; q < TS; ++q) acc[q * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int s0 = tb; s0 < te; s0 += 32) {
     const int nt = min(32, te - s0);
-    // the step's tile indices and row words, all loads in flight together:
-    // group g holds tiles g * TPG + [0, TPG), lane = (tile - g * TPG) * TS + row
     const int my_tc = lane < nt ? __ldg(a.colind + s0 + lane) : 0;
     uint32_t wv[TS];
+    int cnt = 0;
 #pragma unroll
     for (int g = 0; g < TS; ++g) {
-      const int i = g * TPG + lane / TS;
-      wv[g] = i < nt ? tile_row<TS>(a.val, (size_t)(s0 + i), lane % TS) : 0u;
+      wv[g] = k0 + g < nt ? tile_row<TS>(a.val, (size_t)(s0 + k0 + g), r) : 0u;
+      cnt += __popc(wv[g]);
     }
-    int n = 0;
+    const int tot = __reduce_add_sync(0xffffffffu, cnt);
+    if (tot > CAP) {
+      wide_step_dense<TS, DT>(a, s0, nt, my_tc, f0, mine, lane, acc, list);
+      continue;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int pos = incl - cnt;
 #pragma unroll
     for (int g = 0; g < TS; ++g) {
-      if (g * TPG >= nt) break;
       uint32_t w = wv[g];
-      const unsigned nzm = __ballot_sync(0xffffffffu, w != 0);
-      if (nzm == 0) continue;
-      const int cnt = __popc(w);
-      int tot, excl;
-      if (__ballot_sync(0xffffffffu, cnt > 1) == 0) {  // at most one bit per lane
-        tot = __popc(nzm);
-        excl = __popc(nzm & lt_mask);
-      } else {
-        tot = __reduce_add_sync(0xffffffffu, cnt);
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        excl = incl - cnt;
-      }
-      if (n + tot > CAP) {  // warp-uniform; one group's bits always fit in an empty list
-        wide_flush_full<TS, DT>(a, list, n, my_tc, f0, mine, lane, acc);
-        n = 0;
-      }
-      int pos = n + excl;
-      const int i = g * TPG + lane / TS, r = lane % TS;
       while (w) {  // column 0 is the most significant of the TS bits: ascending columns
         const int b = 31 - __clz(w);
-        list[pos++] = (uint16_t)((i << 10) | (r << 5) | (TS - 1 - b));
+        list[pos++] = (uint16_t)(((k0 + g) << 10) | (r << 5) | (TS - 1 - b));
         w &= ~(1u << b);
       }
-      n += tot;
     }
-    wide_flush<TS, DT>(a, list, n, my_tc, f0, mine, lane, acc);
+    wide_flush<TS, DT>(a, list, tot, my_tc, f0, mine, lane, acc);
   }
   if (!mine) return;
-  for (int r = 0; r < TS; ++r) {
-    const long long orow = br * TS + r;
+  for (int q = 0; q < TS; ++q) {
+    const long long orow = br * TS + q;
     if (orow >= a.nrows) break;
-    const float4 v = acc[r * 32 + lane];
+    const float4 v = acc[q * 32 + lane];
     float *dst = a.C + (size_t)orow * a.ldc + f0;
     if (atomic) atomicAdd(reinterpret_cast<float4 *>(dst), v);
     else *reinterpret_cast<float4 *>(dst) = v;

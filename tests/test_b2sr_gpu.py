@@ -274,6 +274,32 @@ def test_b2sr_spmm_float_features_vs_oracle(cuda, ts, F, dtype):
         assert oracle.rel_err(want, ref, mag)[0] <= 1e-5
 
 
+@pytest.mark.parametrize("ts", [16, 32])
+@pytest.mark.parametrize("F,dtype", [(64, torch.float32), (256, torch.float32), (256, torch.bfloat16)])
+def test_b2sr_spmm_dense_tiles(cuda, ts, F, dtype):
+    """Fully dense tiles: rows 0..63 hold every column of a 9,000-column
+    matrix, so a 32-tile step of the tile-wide pass holds more bits than its
+    entry list (the tile-by-tile path) and those block-rows are longer than
+    the cut (segments summed with atomics); the other rows are sparse.
+    Exact against the CSR product on 0/1 features, FP32 rounding against
+    FP64 on float features."""
+    n, m = 500, 9000
+    rng = np.random.default_rng(ts + F)
+    rows = [np.arange(m) if r < 64 else np.sort(rng.choice(m, size=rng.integers(0, 40), replace=False))
+            for r in range(n)]
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(x) for x in rows])
+    ci = np.concatenate(rows).astype(np.int32)
+    A = dev_csr(n, m, rp, ci, cuda)
+    Ab = ops.csr2b2sr(A, ts)
+    B01 = torch.from_numpy(rng.integers(0, 2, (m, F)).astype(np.float32)).to(cuda)
+    assert torch.equal(ops.b2sr_spmm(Ab, B01.to(dtype)), ops.csr_spmm(A, B01))
+    B = G.normal(ts + F, 3, (m, F)).to(dtype)
+    got = ops.b2sr_spmm(Ab, B.to(cuda)).cpu().numpy()
+    ref, mag = oracle.csr_spmm_f64(rp, ci, None, B.float().numpy())
+    assert oracle.rel_err(got, ref, mag)[0] <= 1e-5
+
+
 @pytest.mark.parametrize("F", [32, 64, 256])
 def test_fbf_equals_cusparse_on_pm1(cuda, cusparse_ref, F):
     """The reference driver's own check: B2SR-4 FBF == cusparseSpMM (FP32,
