@@ -674,28 +674,6 @@ __device__ __forceinline__ int2 wide_segments(int T, long long cut) {
   return make_int2(n, (T + n - 1) / n);
 }
 
-// One warp per block-row: a block-row longer than the cut appends its
-// segments (block-row, first tile) to segs, counted in *nsegs, and zeroes its
-// rows of C (F features, ldc = F).
-template <int TS>
-__global__ void k_wide_segments(B2srSpmmArgs a, int *__restrict__ nsegs, int2 *__restrict__ segs) {
-  const long long br = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (br >= a.mb) return;
-  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
-  const long long cut = wide_cut(__ldg(a.rowptr + a.mb), a.slices, a.seg_warps);
-  if (te - tb <= cut) return;
-  const int2 sg = wide_segments(te - tb, cut);
-  int base = 0;
-  if (lane == 0) base = atomicAdd(nsegs, sg.x);
-  base = __shfl_sync(0xffffffffu, base, 0);
-  for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2((int)br, tb + i * sg.y);
-  const long long r0 = br * TS;
-  const int rows = (int)min((long long)TS, (long long)a.nrows - r0);
-  const int F = (int)a.ldc;
-  for (int i = lane; i < rows * F; i += 32) a.C[(r0 + i / F) * a.ldc + i % F] = 0.f;
-}
-
 // 4 features of a B row as FP32 (16-byte FP32 or 8-byte 16-bit load).
 template <int DT>
 __device__ __forceinline__ float4 wide_load(const void *B, size_t elem) {
@@ -712,54 +690,43 @@ __device__ __forceinline__ float4 wide_load(const void *B, size_t elem) {
   }
 }
 
-// Gathers of the n listed entries, WIDE_U at a time, each 4-feature chunk
-// added to its row's sums (entry = tile << 10 | row << 5 | column; the
-// tile's block column is lane `tile`'s tc).
-template <int TS, int DT>
-__device__ __forceinline__ void wide_flush(const B2srSpmmArgs &a, const uint16_t *list, int n, int tc_lane,
-                                           int f0, bool mine, int lane, float4 *acc) {
-  __syncwarp();
-  for (int k0 = 0; k0 < n; k0 += WIDE_U) {
-    float4 x[WIDE_U];
-    int rr[WIDE_U];
-#pragma unroll
-    for (int u = 0; u < WIDE_U; ++u) {
-      const bool live = k0 + u < n;
-      const int e = live ? (int)list[k0 + u] : 0;
-      rr[u] = (e >> 5) & 31;
-      const int tc = __shfl_sync(0xffffffffu, tc_lane, e >> 10);
-      const size_t col = (size_t)(unsigned)tc * TS + (e & 31);
-      x[u] = (live && mine) ? wide_load<DT>(a.B, col * (size_t)a.ldb + f0) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int u = 0; u < WIDE_U; ++u) {
-      if (k0 + u < n) {
-        float4 t = acc[rr[u] * 32 + lane];
-        t.x = t.x + x[u].x;
-        t.y = t.y + x[u].y;
-        t.z = t.z + x[u].z;
-        t.w = t.w + x[u].w;
-        acc[rr[u] * 32 + lane] = t;
-      }
-    }
-  }
-  __syncwarp();
+// One warp per block-row: a block-row longer than the cut appends its
+// segments (block-row, first tile) to segs, counted in *nsegs, and zeroes its
+// rows of C (32-bit elements, F per row).
+template <int TS>
+__global__ void k_wide_segments(const int *__restrict__ rowptr, int mb, int nrows, int F, int slices,
+                                long long warps, uint32_t *__restrict__ C, int *__restrict__ nsegs,
+                                int2 *__restrict__ segs) {
+  const long long br = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (br >= mb) return;
+  const int tb = __ldg(rowptr + br), te = __ldg(rowptr + br + 1);
+  const long long cut = wide_cut(__ldg(rowptr + mb), slices, warps);
+  if (te - tb <= cut) return;
+  const int2 sg = wide_segments(te - tb, cut);
+  int base = 0;
+  if (lane == 0) base = atomicAdd(nsegs, sg.x);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2((int)br, tb + i * sg.y);
+  const long long r0 = br * TS;
+  const int rows = (int)min((long long)TS, (long long)nrows - r0);
+  for (int i = lane; i < rows * F; i += 32) C[(r0 + i / F) * F + i % F] = 0u;
 }
 
 // A step whose bits overflow the list (more than 32 * TS of them), out of
 // line: its tiles one at a time (lane = tile row), flushing whenever the
-// next tile might not fit.  Rows still add in tile and column order.
-template <int TS, int DT>
-__device__ __noinline__ void wide_step_dense(const B2srSpmmArgs &a, int s0, int nt, int tc_lane, int f0, bool mine,
-                                             int lane, float4 *acc, uint16_t *list) {
+// next tile might not fit.  Rows still come in tile and column order.
+template <int TS, class P>
+__device__ __noinline__ void wide_step_dense(const void *val, int s0, int nt, int tc_lane, int lane,
+                                             uint16_t *list, P &body) {
   constexpr int CAP = wide_cap<TS>();
   int n = 0;
   for (int i = 0; i < nt; ++i) {
-    uint32_t w = lane < TS ? tile_row<TS>(a.val, (size_t)(s0 + i), lane) : 0u;
+    uint32_t w = lane < TS ? tile_row<TS>(val, (size_t)(s0 + i), lane) : 0u;
     const int cnt = __popc(w);
     const int tot = __reduce_add_sync(0xffffffffu, cnt);
     if (n + tot > CAP) {  // one tile (TS * TS bits) always fits in an empty list
-      wide_flush<TS, DT>(a, list, n, tc_lane, f0, mine, lane, acc);
+      body.flush(list, n, tc_lane);
       n = 0;
     }
     int incl = cnt;
@@ -776,37 +743,34 @@ __device__ __noinline__ void wide_step_dense(const B2srSpmmArgs &a, int s0, int 
     }
     n += tot;
   }
-  wide_flush<TS, DT>(a, list, n, tc_lane, f0, mine, lane, acc);
+  body.flush(list, n, tc_lane);
 }
 
-// One warp: tiles [tb, te) of block-row br, features [sl * 128, +128).
-// Per step of 32 tiles, lane (k, r) = (lane / TS, lane % TS) loads row r of
-// tiles k * TS + [0, TS) and appends its set bits (tiles ascending, columns
-// ascending) at its place in the list (one prefix sum per step), so every
-// row's entries are in the list in tile and column order.
-template <int TS, int DT>
-__device__ __forceinline__ void wide_block_row(const B2srSpmmArgs &a, long long br, int tb, int te, int sl,
-                                               bool atomic, int lane, float4 *acc, uint16_t *list) {
+// One warp walks tiles [tb, te) of a block-row and hands the set bits to
+// body.flush as (tile, row, column) entries (entry = tile << 10 | row << 5 |
+// column; the tile's block column is lane `tile`'s tc_lane).  Per step of
+// 32 tiles, lane (k, r) = (lane / TS, lane % TS) loads row r of tiles
+// k * TS + [0, TS) (all TS loads in flight together) and writes its set bits
+// (tiles ascending, columns ascending) at its place in the list (one prefix
+// sum per step), so every row's entries are in tile and column order.
+template <int TS, class P>
+__device__ __forceinline__ void wide_walk(const int *colind, const void *val, int tb, int te, int lane,
+                                          uint16_t *list, P &body) {
   constexpr int CAP = wide_cap<TS>();
-  const int F = (int)a.ldc;
-  const int f0 = sl * WIDE_FEATS + lane * 4;
-  const bool mine = f0 < F;  // F % 4 == 0: all 4 features in range
   const int k0 = (lane / TS) * TS, r = lane % TS;
-#pragma unroll
-  for (int q = 0; q < TS; ++q) acc[q * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int s0 = tb; s0 < te; s0 += 32) {
     const int nt = min(32, te - s0);
-    const int my_tc = lane < nt ? __ldg(a.colind + s0 + lane) : 0;
+    const int my_tc = lane < nt ? __ldg(colind + s0 + lane) : 0;
     uint32_t wv[TS];
     int cnt = 0;
 #pragma unroll
     for (int g = 0; g < TS; ++g) {
-      wv[g] = k0 + g < nt ? tile_row<TS>(a.val, (size_t)(s0 + k0 + g), r) : 0u;
+      wv[g] = k0 + g < nt ? tile_row<TS>(val, (size_t)(s0 + k0 + g), r) : 0u;
       cnt += __popc(wv[g]);
     }
     const int tot = __reduce_add_sync(0xffffffffu, cnt);
     if (tot > CAP) {
-      wide_step_dense<TS, DT>(a, s0, nt, my_tc, f0, mine, lane, acc, list);
+      wide_step_dense<TS>(val, s0, nt, my_tc, lane, list, body);
       continue;
     }
     int incl = cnt;
@@ -825,9 +789,60 @@ __device__ __forceinline__ void wide_block_row(const B2srSpmmArgs &a, long long 
         w &= ~(1u << b);
       }
     }
-    wide_flush<TS, DT>(a, list, tot, my_tc, f0, mine, lane, acc);
+    body.flush(list, tot, my_tc);
   }
-  if (!mine) return;
+}
+
+// SpMM body: this lane's 4 features [f0, f0 + 4) of the slice, the TS row
+// sums acc[row * 32 + lane] in shared memory.
+template <int TS, int DT>
+struct WideSpmm {
+  const B2srSpmmArgs &a;
+  int f0, lane;
+  bool mine;
+  float4 *acc;
+  // the n listed entries, WIDE_U gathers at a time, each 4-feature chunk
+  // added to its row's sums
+  __device__ __forceinline__ void flush(const uint16_t *list, int n, int tc_lane) {
+    __syncwarp();
+    for (int k0 = 0; k0 < n; k0 += WIDE_U) {
+      float4 x[WIDE_U];
+      int rr[WIDE_U];
+#pragma unroll
+      for (int u = 0; u < WIDE_U; ++u) {
+        const bool live = k0 + u < n;
+        const int e = live ? (int)list[k0 + u] : 0;
+        rr[u] = (e >> 5) & 31;
+        const int tc = __shfl_sync(0xffffffffu, tc_lane, e >> 10);
+        const size_t col = (size_t)(unsigned)tc * TS + (e & 31);
+        x[u] = (live && mine) ? wide_load<DT>(a.B, col * (size_t)a.ldb + f0) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < WIDE_U; ++u) {
+        if (k0 + u < n) {
+          float4 t = acc[rr[u] * 32 + lane];
+          t.x = t.x + x[u].x;
+          t.y = t.y + x[u].y;
+          t.z = t.z + x[u].z;
+          t.w = t.w + x[u].w;
+          acc[rr[u] * 32 + lane] = t;
+        }
+      }
+    }
+    __syncwarp();
+  }
+};
+
+// One warp: tiles [tb, te) of block-row br, features [sl * 128, +128).
+template <int TS, int DT>
+__device__ __forceinline__ void wide_block_row(const B2srSpmmArgs &a, long long br, int tb, int te, int sl,
+                                               bool atomic, int lane, float4 *acc, uint16_t *list) {
+  const int f0 = sl * WIDE_FEATS + lane * 4;
+  WideSpmm<TS, DT> body{a, f0, lane, f0 < (int)a.ldc, acc};  // F % 4 == 0: all 4 features in range
+#pragma unroll
+  for (int q = 0; q < TS; ++q) acc[q * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+  wide_walk<TS>(a.colind, a.val, tb, te, lane, list, body);
+  if (!body.mine) return;
   for (int q = 0; q < TS; ++q) {
     const long long orow = br * TS + q;
     if (orow >= a.nrows) break;
@@ -960,7 +975,9 @@ gbs_status launch_wide(B2srSpmmArgs &a, cudaStream_t s) {
   GBS_TRY(info.alloc(sizeof(int), s));
   GBS_TRY(segs.alloc(sizeof(int2) * (size_t)a.mb * kSegMax, s));
   GBS_CUDA_TRY(cudaMemsetAsync(info.p, 0, sizeof(int), s));
-  k_wide_segments<TS><<<(int)(((long long)a.mb * 32 + 255) / 256), 256, 0, s>>>(a, info.as<int>(), segs.as<int2>());
+  k_wide_segments<TS><<<(int)(((long long)a.mb * 32 + 255) / 256), 256, 0, s>>>(
+      a.rowptr, a.mb, a.nrows, (int)a.ldc, a.slices, a.seg_warps, reinterpret_cast<uint32_t *>(a.C), info.as<int>(),
+      segs.as<int2>());
   GBS_TRY(check_launch("k_wide_segments"));
   a.hub_info = info.as<int>();
   a.segs = segs.as<int2>();
@@ -989,11 +1006,10 @@ gbs_status b2sr_spmm_wide(int ts, int nrows, int mb, const int *rowptr, const in
     if (dt == DT_BF16) return launch_wide<TS, DT_BF16>(a, s);  \
     return launch_wide<TS, DT_F16>(a, s);                      \
   }
-  GBS_WIDE(8)
   GBS_WIDE(16)
   GBS_WIDE(32)
 #undef GBS_WIDE
-  return fail(GBS_ERR_UNSUPPORTED, "b2sr spmm: the tile-wide pass takes tiles 8, 16 and 32");
+  return fail(GBS_ERR_UNSUPPORTED, "b2sr spmm: the tile-wide pass takes tiles 16 and 32");
 }
 
 }  // namespace
@@ -1354,6 +1370,137 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm_hub_segs(B2srBmmArgs a) {
   }
 }
 
+// Tile-wide BMM (gbs_b2sr_bmm at tile 32, plain layout): the walk
+// of the tile-wide SpMM with integer counts.  An item is a block-row and a
+// slice of 4 feature words (128 features); lane l counts features
+// 32 (w0 + k) + l, k < 4, of every row in acc[row * 32 + l] (shared memory).
+// Each entry adds its feature bits (or 2 bit - 1 for the +-1 form, whose
+// sum is 2 count - entries), so segments of a cut block-row add exactly.
+template <int TS>
+struct WideBmm {
+  const B2srBmmArgs &a;
+  int w0, lane;
+  int4 *acc;
+  __device__ __forceinline__ void flush(const uint16_t *list, int n, int tc_lane) {
+    __syncwarp();
+    const int nwords = min(4, a.W - w0);
+    const int shift = 31 - lane;
+    const int sgn = a.signed_form;
+    for (int k0 = 0; k0 < n; k0 += WIDE_U) {
+      uint32_t x[WIDE_U][4];
+      int rr[WIDE_U];
+#pragma unroll
+      for (int u = 0; u < WIDE_U; ++u) {
+        const bool live = k0 + u < n;
+        const int e = live ? (int)list[k0 + u] : 0;
+        rr[u] = (e >> 5) & 31;
+        const int tc = __shfl_sync(0xffffffffu, tc_lane, e >> 10);
+        const uint32_t *xp = a.X + ((size_t)(unsigned)tc * TS + (e & 31)) * (size_t)a.W + w0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[u][k] = (live && k < nwords) ? __ldg(xp + k) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < WIDE_U; ++u) {
+        if (k0 + u < n) {
+          int b[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            b[k] = (int)((x[u][k] >> shift) & 1u);
+            if (sgn) b[k] = 2 * b[k] - 1;
+          }
+          int4 t = acc[rr[u] * 32 + lane];
+          t.x += b[0];
+          t.y += b[1];
+          t.z += b[2];
+          t.w += b[3];
+          acc[rr[u] * 32 + lane] = t;
+        }
+      }
+    }
+    __syncwarp();
+  }
+};
+
+template <int TS>
+__global__ void __launch_bounds__(WIDE_WARPS * 32, 1) k_b2sr_bmm_wide(B2srBmmArgs a) {
+  extern __shared__ __align__(16) unsigned char wide_sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int4 *acc = reinterpret_cast<int4 *>(wide_sm) + (size_t)warp * TS * 32;
+  uint16_t *list = reinterpret_cast<uint16_t *>(wide_sm + (size_t)WIDE_WARPS * TS * 32 * sizeof(int4)) +
+                   (size_t)warp * wide_cap<TS>();
+  const int slices = (a.W + 3) / 4;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long cut = wide_cut(__ldg(a.rowptr + a.mb), slices, a.seg_warps);
+  const long long main_items = (long long)a.mb * slices;
+  const long long items = main_items + (long long)__ldcg(a.hub_info) * slices;
+  for (long long it = gw; it < items; it += nw) {
+    const int sl = (int)(it % slices);
+    long long br;
+    int tb, te;
+    bool atomic;
+    if (it < main_items) {
+      br = it / slices;
+      tb = __ldg(a.rowptr + br);
+      te = __ldg(a.rowptr + br + 1);
+      if (te - tb > cut) continue;  // done by its segments
+      atomic = false;
+    } else {
+      const int2 sg = a.segs[(it - main_items) / slices];
+      br = sg.x;
+      const int te_row = __ldg(a.rowptr + sg.x + 1);
+      tb = sg.y;
+      te = min(te_row, sg.y + wide_segments(te_row - __ldg(a.rowptr + sg.x), cut).y);
+      atomic = true;
+    }
+    WideBmm<TS> body{a, sl * 4, lane, acc};
+#pragma unroll
+    for (int q = 0; q < TS; ++q) acc[q * 32 + lane] = make_int4(0, 0, 0, 0);
+    wide_walk<TS>(a.colind, a.val, tb, te, lane, list, body);
+    for (int q = 0; q < TS; ++q) {
+      const long long orow = br * TS + q;
+      if (orow >= a.nrows) break;
+      const int4 v = acc[q * 32 + lane];
+      const int vk[4] = {v.x, v.y, v.z, v.w};
+      int32_t *dst = a.C + (size_t)orow * a.F;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int f = (sl * 4 + k) * 32 + lane;
+        if (f < a.F) {
+          if (atomic) atomicAdd(dst + f, vk[k]);
+          else dst[f] = vk[k];
+        }
+      }
+    }
+  }
+}
+
+template <int TS>
+gbs_status launch_bmm_wide(B2srBmmArgs &a, cudaStream_t s) {
+  const void *fn = (const void *)&k_b2sr_bmm_wide<TS>;
+  const size_t smem = wide_smem<TS>();
+  GBS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DeviceInfo di;
+  GBS_TRY(device_info(&di));
+  int per_sm = 0;
+  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WIDE_WARPS * 32, smem));
+  const dim3 grid(di.sm_count * (per_sm > 0 ? per_sm : 1));
+  a.seg_warps = (long long)grid.x * WIDE_WARPS;
+  DevBuf info, segs;
+  GBS_TRY(info.alloc(sizeof(int), s));
+  GBS_TRY(segs.alloc(sizeof(int2) * (size_t)a.mb * kSegMax, s));
+  GBS_CUDA_TRY(cudaMemsetAsync(info.p, 0, sizeof(int), s));
+  k_wide_segments<TS><<<(int)(((long long)a.mb * 32 + 255) / 256), 256, 0, s>>>(
+      a.rowptr, a.mb, a.nrows, a.F, (a.W + 3) / 4, a.seg_warps, reinterpret_cast<uint32_t *>(a.C), info.as<int>(),
+      segs.as<int2>());
+  GBS_TRY(check_launch("k_wide_segments"));
+  a.hub_info = info.as<int>();
+  a.segs = segs.as<int2>();
+  void *args[] = {&a};
+  GBS_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(WIDE_WARPS * 32), args, smem, s));
+  return GBS_OK;
+}
+
 template <int TS, bool AL = false>
 gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   const void *fn = nullptr, *hub_fn = nullptr, *seg_fn = nullptr;
@@ -1384,6 +1531,11 @@ gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   a.hub_info = nullptr;
   a.segs = nullptr;
   a.seg_warps = 1;
+  // plain-layout tile 32: the tile-wide pass (flickr-shaped graph, F = 256
+  // / 1024: 0.77 / 3.02 against 1.54 / 4.02 ms; at tile 16 it lost, 0.77 /
+  // 3.01 against 0.46 / 1.89 ms: each tile is walked once per 4-word slice,
+  // the row kernels above walk it once per row for all words)
+  if constexpr (!AL && TS == 32) return launch_bmm_wide<TS>(a, s);
   if (a.mb < kHubMinBlockRows) {
     void *args[] = {&a};
     GBS_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, s));

@@ -345,6 +345,31 @@ def _bmm_case(cuda, ts, F, gi):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("ts", [16, 32])
+@pytest.mark.parametrize("F", [32, 200, 1024])
+def test_bmm_dense_tiles_bit_exact(cuda, ts, F):
+    """Fully dense tiles through the BMM (tile 32: the tile-wide pass): rows
+    0..63 hold every one of 9,000 columns (steps that overflow the entry
+    list, block-rows cut into segments added with integer atomics), the
+    rest sparse; F = 200 leaves a partial last word.  Unsigned and +-1
+    counts bit for bit against the oracle."""
+    n, m = 500, 9000
+    rng = np.random.default_rng(ts * F)
+    rows = [np.arange(m) if r < 64 else np.sort(rng.choice(m, size=rng.integers(0, 40), replace=False))
+            for r in range(n)]
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(x) for x in rows])
+    ci = np.concatenate(rows).astype(np.int32)
+    brp, bci, bv = oracle.b2sr_pack(n, m, rp, ci, ts)
+    X = G.normal(F + ts, 8, (m, F))
+    Xw = ops.pack_sign_rows(X.to(cuda))
+    Ab = ops.csr2b2sr(dev_csr(n, m, rp, ci, cuda), ts)
+    for signed in (False, True):
+        got = ops.b2sr_bmm(Ab, Xw, F, signed).cpu().numpy()
+        want = oracle.b2sr_bmm(ts, n, brp, bci, bv, Xw.cpu().numpy().view(np.uint32), F, signed)
+        assert np.array_equal(got, want)
+
+
 def test_bmm_signed_matches_fbf_on_pm1(cuda):
     """signed BMM == float FBF product with the +-1 features it encodes."""
     g = G.flickr_like()
