@@ -710,7 +710,10 @@ __global__ void k_wide_segments(const int *__restrict__ rowptr, int mb, int nrow
   for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2((int)br, tb + i * sg.y);
   const long long r0 = br * TS;
   const int rows = (int)min((long long)TS, (long long)nrows - r0);
-  for (int i = lane; i < rows * F; i += 32) C[(r0 + i / F) * F + i % F] = 0u;
+  for (int q = 0; q < rows; ++q) {
+    uint32_t *row = C + (r0 + q) * F;
+    for (int c = lane; c < F; c += 32) row[c] = 0u;
+  }
 }
 
 // A step whose bits overflow the list (more than 32 * TS of them), out of
