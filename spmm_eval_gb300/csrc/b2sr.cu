@@ -570,15 +570,16 @@ __global__ void __launch_bounds__(256, 1) k_b2sr_spmm_hubs(B2srSpmmArgs a) {
 // chains far longer than the mean work of a warp and the SMs idle behind
 // them.  A hub whose walk is longer than 1/kSegShare of the mean work per
 // resident warp (and than kSegMinTiles tiles) is cut into equal segments of
-// consecutive tiles (at most kSegMax); one warp per (segment, tile row,
-// feature slice) adds its partial sums into C, which the segment builder
-// zeroed.  The other hubs go to the ordered pass whole.  Sums of a split hub
-// are formed in an order that depends on scheduling: exact for 0/1 and +-1
-// features (integer partial sums), within FP32 rounding otherwise.
+// consecutive tiles (at most kSegMax); a segment is then an ordinary short
+// block-row: one warp per (segment, group of tile rows) walks it with the
+// main pass's layout (all features, 4 gathers per round, every tile read
+// once per group) and adds its partial sums into C, which the segment
+// builder zeroed.  The other hubs go to the ordered pass whole.  Sums of a
+// split hub are formed in an order that depends on scheduling: exact for 0/1
+// and +-1 features (integer partial sums), within FP32 rounding otherwise.
 constexpr int kSegMax = 64;
 constexpr int kSegMinTiles = 128;
 constexpr int kSegShare = 2;
-constexpr int SEG_U = 8;
 
 // (segments, tiles per segment) of a hub of T tiles; mean_work = tiles of
 // all hubs * items per hub / resident warps.
@@ -611,28 +612,33 @@ __global__ void k_hub_segments(const int *__restrict__ hubs, const int *__restri
   for (int i = lane; i < sg.x; i += 32) segs[base + i] = make_int2(br, tb + i * sg.y);
   const long long r0 = (long long)br * ts;
   const int rows = (int)min((long long)ts, (long long)nrows - r0);
-  for (int i = lane; i < rows * F; i += 32) C[(r0 + i / F) * F + i % F] = 0u;
+  for (int q = 0; q < rows; ++q) {
+    uint32_t *row = C + (r0 + q) * F;
+    for (int c = lane; c < F; c += 32) row[c] = 0u;
+  }
 }
 
-// One warp per (segment, tile row, feature slice), items grid-stride over a
-// grid of resident CTAs; partial sums added into C.
-template <int TS, int DT, int VEC>
-__global__ void __launch_bounds__(256, 2) k_b2sr_spmm_hub_segs(B2srSpmmArgs a) {
+// Segments of cut hubs with the main pass's layout: one warp per (segment,
+// group of R tile rows), all features, items grid-stride over a grid of
+// resident CTAs; partial sums added into C.
+template <int TS, int DT, int VEC, int LPR, int CH, int RPS>
+__global__ void __launch_bounds__(256) k_b2sr_spmm_segs(B2srSpmmArgs a) {
+  constexpr int NSUB = 32 / LPR;
+  constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
+  constexpr int NG = (TS + R - 1) / R;
   const int lane = threadIdx.x & 31;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long per = (long long)TS * a.slices;
-  const long long items = (long long)__ldcg(a.hub_info) * per;
-  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * per / a.seg_warps;
-  __shared__ int2 lists[8][32 * 4];
+  const long long items = (long long)__ldcg(a.hub_info) * NG;
+  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * NG / a.seg_warps;
+  __shared__ int2 lists[8][32 * MAIN_G];
   for (long long it = gw; it < items; it += nw) {
-    const int2 sg = a.segs[it / per];
-    const int r = (int)(it % per);
+    const int2 sg = a.segs[it / NG];
     const int te = __ldg(a.rowptr + sg.x + 1);
     const int len = hub_segments(te - __ldg(a.rowptr + sg.x), mean_work).y;
-    b2sr_block_row<TS, DT, VEC, 32, 1, 1, false, SEG_U, 4, true>(a, sg.x, r / a.slices, (r % a.slices) * HUB_CHUNKS,
-                                                                 lane, lists[threadIdx.x >> 5], sg.y,
-                                                                 min(te, sg.y + len));
+    b2sr_block_row<TS, DT, VEC, LPR, CH, RPS, false, 4, MAIN_G, true>(a, sg.x, (int)(it % NG), 0, lane,
+                                                                      lists[threadIdx.x >> 5], sg.y,
+                                                                      min(te, sg.y + len));
   }
 }
 
@@ -917,7 +923,7 @@ B2srVariant mk_b2sr() {
   constexpr int R = NSUB * RPS < TS ? NSUB * RPS : TS;
   return B2srVariant{(const void *)&k_b2sr_spmm<TS, DT, VEC, LPR, CH, RPS, NZ>, VEC, LPR, CH, R,
                      (TS + R - 1) / R, (const void *)&k_b2sr_spmm_hubs<TS, DT, VEC, NZ>,
-                     NZ ? nullptr : (const void *)&k_b2sr_spmm_hub_segs<TS, DT, VEC>};
+                     NZ ? nullptr : (const void *)&k_b2sr_spmm_segs<TS, DT, VEC, LPR, CH, RPS>};
 }
 
 template <int TS, int DT, int VEC, bool NZ>
@@ -1092,9 +1098,8 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
     a.hub_info = info;
     a.segs = segs.as<int2>();
     a.seg_warps = (long long)seg_grid.x * 8;
-    k_hub_segments<<<(mb + 7) / 8, 256, 0, s>>>(hubs, rowptr, info, segs.as<int2>(), whole.as<int>(),
-                                                (long long)ts * a.slices, a.seg_warps, ts, nrows, F,
-                                                reinterpret_cast<uint32_t *>(C));
+    k_hub_segments<<<(mb + 7) / 8, 256, 0, s>>>(hubs, rowptr, info, segs.as<int2>(), whole.as<int>(), v.groups,
+                                                a.seg_warps, ts, nrows, F, reinterpret_cast<uint32_t *>(C));
     GBS_TRY(check_launch("k_hub_segments"));
     aw.hubs = whole.as<int>();
   }
@@ -1112,7 +1117,7 @@ gbs_status b2sr_spmm_run(int ts, bool store_nz, int nrows, int mb, const int *ro
   cudaError_t e = cudaSuccess;
   if (side1) {
     e = cudaLaunchKernel(v.hub_seg_fn, seg_grid, dim3(256), args, 0, side1);
-    if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_spmm_hub_segs");
+    if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_spmm_segs");
     GBS_CUDA_TRY(cudaEventRecord(ev.e[2], side1));
   }
   // enough warps that every (hub, group, slice) item of a typical graph gets
