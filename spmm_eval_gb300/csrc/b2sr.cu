@@ -1164,8 +1164,12 @@ struct B2srBmmArgs {
 // indices load.  Integer counts: the order of entries does not matter here.
 // AL: the tiles come in the aligned B2SR-8/16 layout (padding tiles carry
 // no bits, so they drop out at the compaction).
-template <int TS, int WMAX, int R, int U, int G, bool AL>
-__device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br, int grp, int lane, int2 *list) {
+// With tb0 >= 0 only tiles [tb0, te0) are walked; ATOMIC adds the counts of
+// the rows with entries (and the +-1 form's additive 2 count - entries) into
+// C.
+template <int TS, int WMAX, int R, int U, int G, bool AL, bool ATOMIC = false>
+__device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br, int grp, int lane, int2 *list,
+                                              int tb0 = -1, int te0 = -1) {
   constexpr int TPG = 32 / TS;
   constexpr int TPS = TPG * G;
   const int row0 = grp * R;
@@ -1178,7 +1182,7 @@ __device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br
 #pragma unroll
     for (int k = 0; k < WMAX; ++k) cnt[i][k] = 0;
   }
-  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
+  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = tb0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
   const int j = lane % TS, l = lane / TS;
   const int shift = 31 - lane;
   int nb[G];
@@ -1238,12 +1242,16 @@ __device__ __forceinline__ void bmm_block_row(const B2srBmmArgs &a, long long br
     const int tr = row0 + i;
     if (tr >= TS) continue;
     const long long orow = br * TS + tr;
-    if (orow >= a.nrows) continue;
+    if (orow >= a.nrows || (ATOMIC && deg[i] == 0)) continue;
     int32_t *dst = a.C + (size_t)orow * a.F;
 #pragma unroll
     for (int k = 0; k < WMAX; ++k) {
       const int c = k * 32 + lane;
-      if (c < a.F) dst[c] = a.signed_form ? 2 * cnt[i][k] - deg[i] : cnt[i][k];
+      const int v = a.signed_form ? 2 * cnt[i][k] - deg[i] : cnt[i][k];
+      if (c < a.F) {
+        if constexpr (ATOMIC) atomicAdd(dst + c, v);
+        else dst[c] = v;
+      }
     }
   }
 }
@@ -1275,12 +1283,9 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm(B2srBmmArgs a) {
 // (entry, word) -- 32 / WMAX entries per warp-wide load, so a round needs
 // WMAX loads per lane and no more registers -- and each word is broadcast to
 // the lanes by a shuffle when its bits are counted.  The chain of dependent
-// round trips is (entries / 32) deep instead of (entries / U).  With
-// tb0 >= 0 only tiles [tb0, te0) are walked; ATOMIC adds the counts (and the
-// +-1 form's 2 * count - entries, which is additive) into C.
-template <int TS, int WMAX, bool AL, bool ATOMIC = false>
-__device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list,
-                                            int tb0 = -1, int te0 = -1) {
+// round trips is (entries / 32) deep instead of (entries / U).
+template <int TS, int WMAX, bool AL>
+__device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, int row, int lane, int2 *list) {
   constexpr int G = 4;
   constexpr int TPG = 32 / TS;
   constexpr int TPS = TPG * G;
@@ -1290,7 +1295,7 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
   int deg = 0;
 #pragma unroll
   for (int k = 0; k < WMAX; ++k) cnt[k] = 0;
-  const int tb = tb0 >= 0 ? tb0 : __ldg(a.rowptr + br), te = tb0 >= 0 ? te0 : __ldg(a.rowptr + br + 1);
+  const int tb = __ldg(a.rowptr + br), te = __ldg(a.rowptr + br + 1);
   const int j = lane % TS, l = lane / TS;
   const int shift = 31 - lane;
   const int my_e = lane / WMAX, my_w = lane % WMAX;  // (entry, word) this lane loads
@@ -1332,16 +1337,12 @@ __device__ __forceinline__ void bmm_hub_row(const B2srBmmArgs &a, long long br, 
     __syncwarp();
   }
   const long long orow = br * TS + row;
-  if (orow >= a.nrows || (ATOMIC && deg == 0)) return;
+  if (orow >= a.nrows) return;
   int32_t *dst = a.C + (size_t)orow * a.F;
 #pragma unroll
   for (int k = 0; k < WMAX; ++k) {
     const int c = k * 32 + lane;
-    const int v = a.signed_form ? 2 * cnt[k] - deg : cnt[k];
-    if (c < a.F) {
-      if constexpr (ATOMIC) atomicAdd(dst + c, v);
-      else dst[c] = v;
-    }
+    if (c < a.F) dst[c] = a.signed_form ? 2 * cnt[k] - deg : cnt[k];
   }
 }
 
@@ -1359,22 +1360,24 @@ __global__ void __launch_bounds__(256) k_b2sr_bmm_hubs(B2srBmmArgs a) {
   }
 }
 
-// Segments of cut hubs (k_hub_segments): one warp per (segment, tile row),
-// counts added into C.
+// Segments of cut hubs (k_hub_segments) with the main pass's layout: one
+// warp per (segment, group of R rows), counts added into C.
 template <int TS, int WMAX, bool AL>
-__global__ void __launch_bounds__(256) k_b2sr_bmm_hub_segs(B2srBmmArgs a) {
+__global__ void __launch_bounds__(256) k_b2sr_bmm_segs(B2srBmmArgs a) {
+  constexpr int R = BmmShape<WMAX>::R0 < TS ? BmmShape<WMAX>::R0 : TS;
+  constexpr int NG = (TS + R - 1) / R;
   const int lane = threadIdx.x & 31;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long items = (long long)__ldcg(a.hub_info) * TS;
-  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * TS / a.seg_warps;
-  __shared__ int2 lists[8][32 * 4];
+  const long long items = (long long)__ldcg(a.hub_info) * NG;
+  const long long mean_work = (long long)__ldcg(a.hub_info + 1) * NG / a.seg_warps;
+  __shared__ int2 lists[8][32 * 2];
   for (long long it = gw; it < items; it += nw) {
-    const int2 sg = a.segs[it / TS];
+    const int2 sg = a.segs[it / NG];
     const int te = __ldg(a.rowptr + sg.x + 1);
     const int len = hub_segments(te - __ldg(a.rowptr + sg.x), mean_work).y;
-    bmm_hub_row<TS, WMAX, AL, true>(a, sg.x, (int)(it % TS), lane, lists[threadIdx.x >> 5], sg.y,
-                                    min(te, sg.y + len));
+    bmm_block_row<TS, WMAX, R, BmmShape<WMAX>::U, 2, AL, true>(a, sg.x, (int)(it % NG), lane,
+                                                               lists[threadIdx.x >> 5], sg.y, min(te, sg.y + len));
   }
 }
 
@@ -1517,7 +1520,7 @@ gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   {                                                          \
     fn = (const void *)&k_b2sr_bmm<TS, WM, AL>;              \
     hub_fn = (const void *)&k_b2sr_bmm_hubs<TS, WM, AL>;     \
-    seg_fn = (const void *)&k_b2sr_bmm_hub_segs<TS, WM, AL>; \
+    seg_fn = (const void *)&k_b2sr_bmm_segs<TS, WM, AL>;     \
     wmax = WM;                                               \
   }
   if (a.W <= 1) GBS_BMM_CASE(1)
@@ -1570,7 +1573,7 @@ gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   a.hub_info = info;
   a.segs = segs.as<int2>();
   a.seg_warps = (long long)seg_grid.x * 8;
-  k_hub_segments<<<(a.mb + 7) / 8, 256, 0, s>>>(hubs, a.rowptr, info, segs.as<int2>(), whole.as<int>(), TS,
+  k_hub_segments<<<(a.mb + 7) / 8, 256, 0, s>>>(hubs, a.rowptr, info, segs.as<int2>(), whole.as<int>(), NG,
                                                 a.seg_warps, TS, a.nrows, a.F, reinterpret_cast<uint32_t *>(a.C));
   GBS_TRY(check_launch("k_hub_segments"));
   B2srBmmArgs aw = a;
@@ -1587,7 +1590,7 @@ gbs_status launch_bmm(B2srBmmArgs &a, cudaStream_t s) {
   void *wargs[] = {&aw};
   gbs_status st = GBS_OK;
   cudaError_t e = cudaLaunchKernel(seg_fn, seg_grid, dim3(256), args, 0, side1);
-  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_bmm_hub_segs");
+  if (e != cudaSuccess) st = cuda_fail(e, "k_b2sr_bmm_segs");
   GBS_CUDA_TRY(cudaEventRecord(ev.e[2], side1));
   e = cudaLaunchKernel(hub_fn, dim3(di.sm_count * 4), dim3(256), wargs, 0, side);
   if (e != cudaSuccess && st == GBS_OK) st = cuda_fail(e, "k_b2sr_bmm_hubs");
