@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(256) k_b2sr_spmm_segs(B2srSpmmArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Tile-wide B2SR SpMM (gbs_b2sr_spmm, tiles 8 / 16 / 32).  The kernels above
+// Tile-wide B2SR SpMM (gbs_b2sr_spmm, tiles 16 / 32).  The kernels above
 // give a warp R rows of a block-row, so at large tiles every tile is walked
 // TS / R times (and TS times in the hub pass): at tile 32 the walk of the
 // tile indices and row words, not the gathers, is the work.  Here one warp
