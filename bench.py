@@ -328,7 +328,8 @@ def other_configs(dev, timed, reps):
     each rep): the 4096-row uniform matrix (F = 32); the 89,250-node
     flickr-shaped graph (CSR SpMM at F = 32..256, CSR -> B2SR packing and
     B2SR x FP32 SpMM at tiles 4/8/16/32, B2SR x bits BMM at F = 32..1024); the
-    8192^3-bit binary GEMM; one GCN layer Y = A (X W) forward + backward on
+    8192^3-bit binary GEMM beside cuBLASLt's dense FP8 GEMM of the same shape
+    (its tensor-pipe ceiling); one GCN layer Y = A (X W) forward + backward on
     the normalised flickr-shaped graph (X 89,250 x 512, W 512 x 128)."""
     import torch
     from spmm_eval_gb300 import graphs as G
@@ -407,6 +408,20 @@ def other_configs(dev, timed, reps):
                        "bin_words_fused_ms": round(ms_bin, 4), "bin_words_two_pass_ms": round(ms_bin2, 4),
                        "timeouts": ops.bmm_tc_timeouts()}
     del Aw, Bw, words
+    # The tensor-pipe rate the bit GEMM (bits expanded to e4m3) can reach on this GPU: cuBLASLt's
+    # dense FP8 GEMM of the same shape (torch._scaled_mm, e4m3 x e4m3 -> bf16), measured here.
+    try:
+        fa = torch.randn(8192, 8192, device=dev).to(torch.float8_e4m3fn)
+        fb = torch.randn(8192, 8192, device=dev).to(torch.float8_e4m3fn).t()
+        one = torch.tensor(1.0, device=dev)
+        ms_fp8 = mean_ms(timed, lambda: torch._scaled_mm(fa, fb, scale_a=one, scale_b=one,
+                                                         out_dtype=torch.bfloat16), reps, "fp8_gemm8192")
+        out["bmm_8192"]["fp8_gemm_cublaslt"] = {
+            "ms": round(ms_fp8, 4), "pflops": round(2 * 8192 ** 3 / (ms_fp8 * 1e-3) / 1e15, 3),
+            "bit_gemm_frac": round(ms_fp8 / ms, 3)}
+        del fa, fb
+    except (RuntimeError, AttributeError, TypeError) as ex:
+        out["bmm_8192"]["fp8_gemm_cublaslt"] = {"unavailable": repr(ex)[:160]}
 
     # GCN layer on the normalised flickr-shaped graph
     gn = G.gcn_normalize(g)
