@@ -663,7 +663,7 @@ constexpr int WIDE_U = 8;        // gathers in flight per lane
 constexpr int kWideCutMin = 256; // tiles: shorter block-rows are never cut
 
 template <int TS>
-constexpr int wide_cap() { return 32 * TS; }  // list entries: the bits of 32 / TS tiles at most
+constexpr int wide_cap() { return 32 * TS; }  // list entries (a step with more bits goes tile by tile)
 template <int TS>
 constexpr size_t wide_smem() {
   return (size_t)WIDE_WARPS * (TS * 32 * sizeof(float4) + wide_cap<TS>() * sizeof(uint16_t));
