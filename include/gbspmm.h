@@ -205,7 +205,8 @@ GBS_API gbs_status gbs_degree_rsqrt(int nrows, const int *d_rowptr, float *d_out
  * copies in, C = A * B, copies out, and returns when h_C is filled.  A is
  * sent in row ranges of ~nnz/16 nonzeros so the copies overlap the kernels
  * (pinned host buffers are needed for the overlap; pageable ones work,
- * serialised).  ctx (optional) keeps device buffers, streams and events
+ * serialised); the ranges' kernels alternate between `stream` and a
+ * library-owned compute stream so one range's tail overlaps the next.  ctx (optional) keeps device buffers, streams and events
  * between calls; with ctx == NULL each call allocates its buffers
  * stream-ordered on `stream`.  A context serves one call at a time. */
 typedef struct gbs_spmm_host_ctx gbs_spmm_host_ctx;
